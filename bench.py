@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Benchmark of the TeaLeaf implicit solve on GB300.
+
+Workload: the standard five-state deck (10 x 10 domain, dt 0.004) at
+4096 x 4096 cells, FP64 CG with the diagonal Jacobi preconditioner, solved to
+tl_eps 1e-15 with tl_max_iters 10000.  A step is one timestep: one complete
+implicit solve (tea_leaf(), tea_solve.f90:37) plus the field summary, with
+every field resident in HBM.  The metric is cell-iterations per second:
+cells x solver iterations / time, summed over the K timed steps; the time to
+solution per step is reported beside it.
+
+Legs (all in one run, one JSON line):
+  value      K device-resident solves (CUDA graphs), timed with CUDA events on
+             the library's stream, fields resident in HBM.  Every field of the
+             4096^2 problem is larger than L2 (134 MB each), so no flush is
+             needed between steps.
+  roofline   K more solves with per-kernel CUDA events (eager launches); the
+             dominant kernel's algorithmic bytes per launch / its mean launch
+             time, against the measured HBM copy bandwidth.
+  e2e        K more solves through the C-ABI with host buffers: density and
+             energy copied host->device before and energy copied back after
+             every solve, inside the timed region.
+  cpu_baseline  the CPU oracle (oracle/) on the host cores, one timestep of
+             the same deck capped at a fixed iteration count.
+
+--impl reference runs the reference algorithm on the host CPU instead (the
+reference has no CPU implementation of this path, so the oracle's
+restatement of it is timed, all host threads), on the same deck, each step a
+timestep capped at --ref-iters iterations.
+
+Multi-GPU: one process per GPU (torchrun); each rank solves its own replica
+(the single-chunk solve has no data-parallel split), value = all ranks'
+cell-iterations / the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-solution & cell-iters/s at tl_eps: mixed+learned vs plain FP64 CG, 1 GB300"
+
+STATES = """state 1 density=100.0 energy=0.0001
+state 2 density=0.1 energy=25.0 geometry=rectangle xmin=0.0 xmax=1.0 ymin=1.0 ymax=2.0
+state 3 density=0.1 energy=0.1 geometry=rectangle xmin=1.0 xmax=6.0 ymin=1.0 ymax=2.0
+state 4 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=6.0 ymin=1.0 ymax=8.0
+state 5 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=10.0 ymin=7.0 ymax=8.0
+"""
+
+# algorithmic bytes per interior cell of each FP64 kernel: every array the
+# kernel must read or write, counted once (halos ignored)
+BYTES_PER_CELL = {
+    "cg_w": 32,          # read p, Kx, Ky; write w
+    "cg_ur": 64,         # jac_diag: read u, p, r, w, Mi; write u, r, z
+    "cg_p": 24,          # read z, p; write p
+    "residual": 40,      # read u, u0, Kx, Ky; write r
+    "cg_init": 48,       # read r, Kx, Ky; write Mi, z, p
+    "common_init": 56,   # read density, energy; write Kx, Ky, u, u0
+    "field_summary": 32,
+    "finalise": 24,
+}
+
+
+def make_deck(n, solver="cg", precond="jac_diag", max_iters=10000, end_step=100000, precision="fp64"):
+    return ("*tea\n" + STATES +
+            f"x_cells={n}\ny_cells={n}\nxmin=0.0\nymin=0.0\nxmax=10.0\nymax=10.0\n"
+            f"initial_timestep=0.004\nend_step={end_step}\ntl_max_iters={max_iters}\n"
+            f"tl_use_{solver}\ntl_preconditioner_type {precond}\ntl_eps 1.0e-15\n"
+            f"tl_precision {precision}\nsummary_frequency 0\n*endtea\n")
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ distributed
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    dist.init_process_group("nccl" if os.environ.get("TL_BENCH_GLOO") is None else "gloo")
+    return rank, ws, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, ws, local):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x, ws, local):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- oracle
+def oracle_sample(n, iters, steps, threads=None):
+    """Run the CPU oracle on the deck capped at `iters` iterations per step;
+    returns per-step (iterations, wall seconds)."""
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    exe = os.path.join(ROOT, "oracle", "_build", "tea_oracle")
+    with tempfile.NamedTemporaryFile("w", suffix=".in", delete=False) as f:
+        f.write(make_deck(n, max_iters=iters, end_step=steps))
+        path = f.name
+    env = dict(os.environ)
+    env["OMP_NUM_THREADS"] = str(threads or os.cpu_count())
+    env.setdefault("OMP_PROC_BIND", "close")
+    try:
+        out = subprocess.run([exe, path], check=True, capture_output=True, text=True, env=env).stdout
+    finally:
+        os.unlink(path)
+    recs = [json.loads(l) for l in out.splitlines() if l.strip()]
+    steps_r = [r for r in recs if r["kind"] == "step" and r["step"] > 0]
+    walls, prev = [], 0.0
+    for r in steps_r:
+        walls.append(r["wall"] - prev)
+        prev = r["wall"]
+    return [(r["iterations"], w) for r, w in zip(steps_r, walls)], recs[-1]["threads"]
+
+
+def run_reference(args):
+    rank, ws, local = dist_init()
+    if rank != 0:
+        return
+    n = args.n
+    per, threads = oracle_sample(n, args.ref_iters, args.warmup + args.steps)
+    timed = per[args.warmup:]
+    its = sum(i for i, _ in timed)
+    secs = sum(w for _, w in timed)
+    value = n * n * its / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-iters/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / len(timed), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (standard five-state deck)",
+        "config": {"workload": f"standard deck {n}x{n}, CG + jac_diag, FP64, tl_eps 1e-15, "
+                               f"each step one timestep capped at {args.ref_iters} iterations",
+                   "parallelism": "cpu", "cells": n * n},
+        "cpu_baseline": {"value": value, "unit": "cell-iters/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} timesteps of the {n}^2 deck, {args.ref_iters} "
+                                   "CG iterations each, CPU oracle (C, OpenMP)"},
+        "e2e": {"value": value, "unit": "cell-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- ours
+def run_ours(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import tealeaf_cuda_gb300 as tl
+
+    rank, ws, local = dist_init()
+    torch.cuda.set_device(local)
+    lib = tl.load()
+    n = args.n
+    deck = make_deck(n, solver=args.solver, precond=args.precond, precision=args.precision)
+    cfg = tl.parse_deck(deck)
+    cfg.cuda_device = local
+    ch = tl.Chunk(cfg)
+    ch.start()
+    stream = torch.cuda.ExternalStream(lib.tl_chunk_stream(ch._h), device=local)
+    cells = n * n
+
+    for _ in range(args.warmup):
+        ch.timestep()
+
+    # ---- value: device-resident solves, CUDA events on the library stream
+    barrier(ws)
+    torch.cuda.synchronize()
+    launches0 = ch.kernel_launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    its = []
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            its.append(ch.timestep()["iterations"])
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    launches = ch.kernel_launches - launches0
+    clocks = clk.summary()
+    ms_max = allreduce_max(ms, ws, local)
+    total_cell_its = allreduce_sum(float(cells * sum(its)), ws, local)
+    value = total_cell_its / (ms_max * 1e-3)
+
+    # ---- roofline: per-kernel CUDA events over K more solves
+    lib.tl_set_profiling(ch._h, 1)
+    lib.tl_profile_reset(ch._h)
+    prof_its = 0
+    for _ in range(args.steps):
+        prof_its += ch.timestep()["iterations"]
+    kernels = {}
+    k = 0
+    while True:
+        name, cnt, kms = C.c_char_p(), C.c_longlong(), C.c_double()
+        if lib.tl_profile_read(ch._h, k, C.byref(name), C.byref(cnt), C.byref(kms)) != 0:
+            break
+        if cnt.value:
+            kernels[name.value.decode()] = {"launches": cnt.value, "ms": kms.value}
+        k += 1
+    lib.tl_set_profiling(ch._h, 0)
+    total_kms = sum(v["ms"] for v in kernels.values()) or 1.0
+    dom = max(kernels, key=lambda x: kernels[x]["ms"])
+    dom_launch_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
+    bytes_per_launch = BYTES_PER_CELL.get(dom, 0) * cells
+    achieved = bytes_per_launch / (dom_launch_ms * 1e-3) / 1e9
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src,
+                "traffic": args.traffic_per_launch,
+                "bytes_per_cell": BYTES_PER_CELL.get(dom), "launch_ms": dom_launch_ms,
+                "kernel_share": {k2: round(v["ms"] / total_kms, 4) for k2, v in
+                                 sorted(kernels.items(), key=lambda kv: -kv[1]["ms"])},
+                "measured_over": f"{args.steps} solves, eager launches with per-kernel CUDA events"}
+
+    # ---- e2e: host buffers through the C-ABI, copies inside the timed region
+    shape = ch.shape
+    host_rho = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    host_e = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    host_rho[:] = ch.get_field("density")
+    host_e[:] = ch.get_field("energy1")
+    h2d = 2 * host_rho.nbytes
+    d2h = host_e.nbytes
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_its = 0
+    for _ in range(args.steps):
+        ch.set_field("density", host_rho)
+        ch.set_field("energy1", host_e)
+        e2e_its += ch.timestep()["iterations"]
+        host_e[:] = ch.get_field("energy1")
+    torch.cuda.synchronize()
+    e2e_s = allreduce_max(time.perf_counter() - t0, ws, local)
+    e2e_total = allreduce_sum(float(cells * e2e_its), ws, local)
+    e2e = {"value": e2e_total / e2e_s, "unit": "cell-iters/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps}
+    ch.close()
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        per, threads = oracle_sample(n, args.cpu_iters, 1)
+        it0, w0 = per[0]
+        cpu = {"value": cells * it0 / w0, "unit": "cell-iters/s", "cores": threads, "kind": "port",
+               "sample": f"one timestep of the {n}^2 deck capped at {args.cpu_iters} CG+jac_diag "
+                         f"iterations ({it0} run, {w0:.1f} s), CPU oracle (C, OpenMP)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "cell-iters/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (standard five-state deck of the reference benchmarks)",
+            "config": {"workload": f"standard deck {n}x{n}, {args.solver.upper()} + {args.precond}, "
+                                   f"{args.precision}, tl_eps 1e-15, one timestep per step",
+                       "cells": cells, "iterations_per_step": its,
+                       "time_to_solution_ms_per_step": ms_max / args.steps,
+                       "l2": "fields larger than L2 (134 MB each), no flush",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--solver", default="cg", choices=["cg", "ppcg", "chebyshev"])
+    ap.add_argument("--precond", default="jac_diag", choices=["none", "jac_diag", "jac_block"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--ref-iters", type=int, default=200)
+    ap.add_argument("--cpu-iters", type=int, default=1500)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic-per-launch", type=float, default=None,
+                    help="dram bytes per launch of the dominant kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

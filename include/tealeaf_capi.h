@@ -1,0 +1,284 @@
+/*
+ * tealeaf_capi.h -- C-ABI of libtealeaf_gb300.so, the GB300 (sm_103a) CUDA
+ * implementation of TeaLeaf's implicit heat-conduction solve.
+ *
+ * Two layers:
+ *
+ *  1. The reference's own entry points, same symbol names and by-reference
+ *     arguments as the gfortran-mangled `*_kernel_cuda_` functions of
+ *     UK-MAC/TeaLeaf_CUDA, so the unchanged Fortran wrappers (tea_leaf_cg.f90,
+ *     tea_leaf_common.f90, tea_leaf_ppcg.f90, tea_leaf_cheby.f90,
+ *     field_summary.f90, update_halo.f90, build_field.f90, generate_chunk.f90,
+ *     initialise_chunk.f90, set_field.f90) link against this library in place
+ *     of the reference's *_kernel_cuda.cu objects.  Each comment cites the
+ *     reference definition it replaces.  They act on one process-wide chunk,
+ *     created by initialise_cuda_, exactly like the reference's `cuda_chunk`
+ *     singleton (init_cuda.cu:33).  They return nothing, as in the reference;
+ *     an error is recorded and can be read with tl_last_error().
+ *
+ *  2. The `tl_*` API: explicit chunk handles, an explicit configuration
+ *     struct instead of the reference's second scan of ./tea.in
+ *     (init_cuda.cu:63-163), integer status codes, and a device-resident
+ *     solve (tl_timestep) that keeps alpha/beta and the exit test on the GPU.
+ *
+ * All device memory is owned by the library; callers pass host scalars and
+ * host arrays only.  Fields crossing the boundary use the reference layout:
+ * (x_cells + 2*halo) columns by (y_cells + 2*halo) rows, x fastest, as
+ * THARR2D of kernel_files/cuda_kernel_header.hpp:27-29.
+ */
+#ifndef TEALEAF_CAPI_H
+#define TEALEAF_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define TL_OK                    0
+#define TL_WARN_MAXITER          1  /* tl_max_iters reached before tl_eps   */
+#define TL_ERR_ARG              -1  /* bad argument or configuration        */
+#define TL_ERR_CUDA             -2  /* a CUDA runtime call failed           */
+#define TL_ERR_ALLOC            -3  /* device or host allocation failed     */
+#define TL_ERR_BREAKDOWN        -4  /* NaN/Inf in a Krylov scalar           */
+#define TL_ERR_STATE            -5  /* call out of order (no chunk, ...)    */
+#define TL_ERR_DECK             -6  /* tea.in could not be parsed           */
+#define TL_ERR_EIGEN            -7  /* eigenvalue estimate failed           */
+
+/* ------------------------------------------------------------ enumerations
+ * values as the reference: data.f90:62-75, cuda_common.hpp:32-55 */
+#define TL_SOLVER_JACOBI         1
+#define TL_SOLVER_CG             2
+#define TL_SOLVER_CHEBYSHEV      3
+#define TL_SOLVER_PPCG           4
+#define TL_PREC_NONE             1
+#define TL_PREC_JAC_DIAG         2
+#define TL_PREC_JAC_BLOCK        3
+#define TL_COEF_CONDUCTIVITY     1
+#define TL_COEF_RECIP_CONDUCTIVITY 2
+#define TL_GEOM_RECTANGLE        1
+#define TL_GEOM_CIRCLE           2
+#define TL_GEOM_POINT            3
+/* numerical form of the solve (no reference counterpart) */
+#define TL_PRECISION_FP64        0  /* plain FP64: the drop-in               */
+#define TL_PRECISION_MIXED       1  /* FP32 inner Krylov + FP64 refinement   */
+/* field ids: FIELD_* of data.f90:44-50 plus solver work arrays */
+#define TL_FIELD_DENSITY         1
+#define TL_FIELD_ENERGY0         2
+#define TL_FIELD_ENERGY1         3
+#define TL_FIELD_U               4
+#define TL_FIELD_P               5
+#define TL_FIELD_SD              6
+#define TL_FIELD_R               7
+#define TL_FIELD_U0              8
+#define TL_FIELD_W               9
+#define TL_FIELD_Z              10
+#define TL_FIELD_KX             11
+#define TL_FIELD_KY             12
+#define TL_FIELD_MI             13
+#define TL_FIELD_CP             14
+#define TL_FIELD_BFP            15
+#define TL_FIELD_VOLUME         16
+#define TL_FIELD_RTEMP          17
+#define TL_FIELD_UTEMP          18
+#define TL_FIELD_R_STORE        19
+
+#define TL_MAX_STATES           64
+
+typedef struct tl_state {
+    int geometry;                 /* TL_GEOM_*                               */
+    double density, energy;
+    double xmin, xmax, ymin, ymax, radius;
+} tl_state_t;
+
+/* Everything tea.in sets (read_input.f90:38-327).  State extents are stored
+ * after read_input.f90:320-327 shrinks states 2..N by a hundredth of a cell. */
+typedef struct tl_config {
+    int x_cells, y_cells;
+    double xmin, xmax, ymin, ymax;
+    double dtinit, end_time;
+    int end_step, summary_frequency;
+    int max_iters;                /* tl_max_iters                            */
+    double eps;                   /* tl_eps                                  */
+    int solver;                   /* TL_SOLVER_*                             */
+    int precond;                  /* TL_PREC_*                               */
+    int coefficient;              /* TL_COEF_*                               */
+    int halo_depth;
+    int reflective_boundary;
+    int check_result;             /* tl_check_result                         */
+    int ch_cg_presteps;           /* tl_ch_cg_presteps                       */
+    double ch_cg_epslim;          /* tl_ch_cg_epslim                         */
+    int ppcg_inner_steps;         /* tl_ppcg_inner_steps                     */
+    int profiler_on, verbose, test_problem, cuda_device;
+    int precision;                /* TL_PRECISION_* (tl_precision)           */
+    double inner_eps;             /* mixed: inner FP32 relative tolerance    */
+    int nstates;
+    tl_state_t states[TL_MAX_STATES];
+} tl_config_t;
+
+/* outcome of one implicit solve (one call of tea_leaf(), tea_solve.f90:37) */
+typedef struct tl_solve_info {
+    int status;                   /* TL_OK, TL_WARN_MAXITER or an error      */
+    int iterations;               /* "Iteration count" (tea_solve.f90:452)   */
+    int ppcg_inner_iters;         /* "PPCG Iteration count" (:457)           */
+    int switch_n;                 /* CG iteration of the Chebyshev/PPCG switch */
+    int est_itc;                  /* Chebyshev iteration estimate            */
+    int outer_iters;              /* mixed: FP64 refinement steps            */
+    int inner_iters;              /* mixed: FP32 Krylov iterations in total  */
+    double initial_residual;
+    double error;                 /* final |error|                           */
+    double error_ratio;           /* "Conduction error" (tea_solve.f90:446)  */
+    double exact_error_ratio;     /* tl_check_result (tea_solve.f90:449)     */
+    double eigmin, eigmax;
+    double rx, ry;
+    double seconds;               /* wall time of the solve on the host      */
+} tl_solve_info_t;
+
+typedef struct tl_chunk tl_chunk_t;
+
+/* ------------------------------------------------------------- tl_* API */
+
+/* tea.in text -> config, with parse.f90 / read_input.f90 semantics */
+int tl_parse_deck(const char *deck_text, tl_config_t *cfg, char *err, int errlen);
+/* message of the most recent error on this thread ("" if none) */
+const char *tl_last_error(void);
+void tl_clear_error(void);
+/* library version string */
+const char *tl_version(void);
+/* sizeof of the public structs, for bindings that mirror them:
+ * 0 tl_config_t, 1 tl_solve_info_t, 2 tl_step_record_t, 3 tl_run_options_t,
+ * 4 tl_run_result_t, 5 tl_state_t; -1 for an unknown id */
+long long tl_sizeof(int which);
+
+/* allocate a chunk for cfg on cfg->cuda_device (all device memory) */
+int tl_chunk_create(const tl_config_t *cfg, tl_chunk_t **out);
+int tl_chunk_destroy(tl_chunk_t *ch);
+/* start.f90:25-112: mesh, states, set_field, then the step-0 field summary */
+int tl_start(tl_chunk_t *ch, double *vol, double *mass, double *ie, double *temp);
+/* one implicit solve at the chunk's dt (tea_solve.f90:37-509), on the
+ * device-resident path; does not advance time */
+int tl_timestep(tl_chunk_t *ch, tl_solve_info_t *info);
+/* field_summary.f90:27-115 kernel part: sums over the interior */
+int tl_field_summary(tl_chunk_t *ch, double *vol, double *mass, double *ie, double *temp);
+/* copy a field between the device and a host array in the reference layout */
+int tl_get_field(tl_chunk_t *ch, int field, double *host);
+int tl_set_field(tl_chunk_t *ch, int field, const double *host);
+/* current dt of the chunk (timestep.f90 / calc_dt.f90) */
+int tl_set_dt(tl_chunk_t *ch, double dt);
+/* number of kernels this chunk has launched so far */
+long long tl_kernel_launches(tl_chunk_t *ch);
+/* the cudaStream_t all of this chunk's work runs on (for caller-side events) */
+void *tl_chunk_stream(tl_chunk_t *ch);
+/* per-kernel timing: when on, solves launch kernels one by one (no graph)
+ * with a CUDA event pair around each; tl_profile_read returns, per kernel
+ * name index idx = 0, 1, ..., the launch count and total milliseconds
+ * (TL_ERR_ARG past the last name) */
+int tl_set_profiling(tl_chunk_t *ch, int on);
+int tl_profile_reset(tl_chunk_t *ch);
+int tl_profile_read(tl_chunk_t *ch, int idx, const char **name, long long *launches, double *ms);
+/* the process-wide chunk the reference-named entry points act on */
+tl_chunk_t *tl_default_chunk(void);
+/* create that chunk from an explicit configuration (initialise_cuda_ does
+ * the same from ./tea.in) */
+int tl_default_chunk_init(const tl_config_t *cfg);
+
+/* ------------------------------------------------------- whole program
+ * The main program of the reference (tea_leaf.f90 -> start.f90 ->
+ * diffuse.f90) restated in C++: read a deck, set up the chunk, run the
+ * timestep loop, print the reference's tea.out lines. */
+typedef struct tl_step_record {
+    int step;
+    double time, dt;
+    tl_solve_info_t solve;
+    int has_summary;
+    double vol, mass, ie, temp;
+    double wall;                  /* seconds since the first timestep began  */
+} tl_step_record_t;
+
+typedef struct tl_run_options {
+    const char *out_path;         /* tea.out to write, or NULL               */
+    int echo;                     /* also write the log to stdout            */
+    int legacy_abi;               /* 1: drive the reference-named entry
+                                     points with the host control flow of
+                                     tea_solve.f90, as the Fortran does      */
+    int max_steps;                /* stop early after this many steps (0: no) */
+    tl_step_record_t *records;    /* optional, one per step (step 0 first)   */
+    int max_records;
+} tl_run_options_t;
+
+typedef struct tl_run_result {
+    int status;
+    int steps;
+    long long total_iterations;
+    double wall_seconds;          /* the whole timestep loop                 */
+    double solve_seconds;         /* sum of the implicit solves              */
+    double vol, mass, ie, temp;   /* final field summary                     */
+    int qa_checked, qa_passed;    /* field_summary.f90:92-112                */
+    double qa_diff;
+    long long kernel_launches;
+    int n_records;
+} tl_run_result_t;
+
+int tl_run_deck(const char *deck_text, const tl_run_options_t *opt, tl_run_result_t *res);
+
+/* ------------------------------------------- reference entry points (1) */
+
+/* init_cuda.cu:35 (INITIALISE_ARGS): create the chunk; solver,
+ * preconditioner, halo depth, profiler and device come from ./tea.in as in
+ * init_cuda.cu:63-163 */
+void initialise_cuda_(int *x_min, int *x_max, int *y_min, int *y_max);
+/* initialise_chunk_kernel_cuda.cu:28 */
+void initialise_chunk_kernel_cuda_(double *d_xmin, double *d_ymin, double *d_dx, double *d_dy);
+/* generate_chunk_kernel_cuda.cu:28 */
+void generate_chunk_kernel_cuda_(const int *number_of_states, const double *state_density,
+                                 const double *state_energy, const double *state_xmin,
+                                 const double *state_xmax, const double *state_ymin,
+                                 const double *state_ymax, const double *state_radius,
+                                 const int *state_geometry, const int *g_rect, const int *g_circ,
+                                 const int *g_point);
+/* set_field_kernel_cuda.cu:4 */
+void set_field_kernel_cuda_(void);
+/* field_summary_kernel_cuda.cu:30 */
+void field_summary_kernel_cuda_(double *vol, double *mass, double *ie, double *temp);
+/* update_halo_kernel_cuda.cu:31 (fields indexed by FIELD_* - 1) */
+void update_halo_kernel_cuda_(const int *chunk_neighbours, const int *fields, const int *depth);
+/* pack_kernel_cuda.cu:7,14: MPI halo packing; a single chunk has no
+ * neighbours, so these only record an error if ever called */
+void cuda_pack_buffers_(int *fields, int *offsets, int *depth, int *face, double *host_buffer);
+void cuda_unpack_buffers_(int *fields, int *offsets, int *depth, int *face, double *host_buffer);
+/* tea_leaf_kernel_cuda.cu:233 (rx, ry are outputs) */
+void tea_leaf_common_init_kernel_cuda_(const int *coefficient, double *dt, double *rx,
+                                       double *ry, int *zero_boundary, int *reflective_boundary);
+/* tea_leaf_kernel_cuda.cu:242 */
+void tea_leaf_common_finalise_kernel_cuda_(void);
+/* tea_leaf_kernel_cuda.cu:248 */
+void tea_leaf_calc_residual_cuda_(void);
+/* tea_leaf_kernel_cuda.cu:34 (norm_array 0: u0.u0, 1: r.r, 2: r.z) */
+void tea_leaf_calc_2norm_kernel_cuda_(int *norm_array, double *norm);
+/* tea_leaf_kernel_cuda.cu:140,146,151,156 */
+void tea_leaf_cg_init_kernel_cuda_(double *rro);
+void tea_leaf_cg_calc_w_kernel_cuda_(double *pw);
+void tea_leaf_cg_calc_ur_kernel_cuda_(double *alpha, double *rrn);
+void tea_leaf_cg_calc_p_kernel_cuda_(double *beta);
+/* tea_leaf_kernel_cuda.cu:42,50 */
+void tea_leaf_cheby_init_kernel_cuda_(const double *ch_alphas, const double *ch_betas,
+                                      int *n_coefs, const double *theta);
+void tea_leaf_cheby_iterate_kernel_cuda_(const int *cheby_calc_step);
+/* tea_leaf_kernel_cuda.cu:301,309,315,322,330,336,342,349,488,503 */
+void tea_leaf_ppcg_init_constants_cuda_(const double *ch_alphas, const double *ch_betas,
+                                        int *n_inner_steps);
+void tea_leaf_ppcg_init_kernel_cuda_(const int *step, double *rro);
+void tea_leaf_ppcg_init_sd_kernel_cuda_(const double *theta);
+void tea_leaf_ppcg_init_sd_new_kernel_cuda_(const double *theta);
+void tea_leaf_ppcg_store_r_kernel_cuda_(void);
+void tea_leaf_ppcg_update_z_kernel_cuda_(void);
+void tea_leaf_ppcg_calc_rrn_kernel_cuda_(double *norm);
+void tea_leaf_ppcg_inner_kernel_cuda_(int *ppcg_cur_step, int *bounds_extra, int *chunk_neighbours);
+void tea_leaf_ppcg_calc_2norm_kernel_cuda_(double *norm);
+void tea_leaf_ppcg_calc_p_kernel_cuda_(double *beta);
+/* tea_leaf_kernel_cuda.cu:215 */
+void tea_leaf_jacobi_solve_kernel_cuda_(double *error);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TEALEAF_CAPI_H */

@@ -1,0 +1,538 @@
+// tl_chunk.cu -- chunk runtime: device memory, mesh, fields, errors and the
+// tl_* handle API.  Replaces the reference's TealeafCudaChunk
+// (cuda_common.hpp:202-388, init_cuda.cu:50-413): one stream per chunk,
+// 256-byte aligned rows, status codes instead of MPI_Abort.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "tl_internal.cuh"
+
+namespace tl {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? TL_ERR_ALLOC : TL_ERR_CUDA;
+}
+
+double *field_ptr(Chunk *c, int field) {
+    switch (field) {
+    case TL_FIELD_DENSITY: return c->density;
+    case TL_FIELD_ENERGY0: return c->energy0;
+    case TL_FIELD_ENERGY1: return c->energy1;
+    case TL_FIELD_U: return c->u;
+    case TL_FIELD_P: return c->p;
+    case TL_FIELD_SD: return c->sd;
+    case TL_FIELD_R: return c->r;
+    case TL_FIELD_U0: return c->u0;
+    case TL_FIELD_W: return c->w;
+    case TL_FIELD_Z: return c->z;
+    case TL_FIELD_KX: return c->kx;
+    case TL_FIELD_KY: return c->ky;
+    case TL_FIELD_MI: return c->mi;
+    case TL_FIELD_CP: return c->cp;
+    case TL_FIELD_BFP: return c->bfp;
+    case TL_FIELD_VOLUME: return c->volume;
+    case TL_FIELD_RTEMP: return c->rtemp;
+    case TL_FIELD_UTEMP: return c->utemp;
+    case TL_FIELD_R_STORE: return c->r_store;
+    default: return nullptr;
+    }
+}
+
+static int dalloc(Chunk *c, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    c->allocations.push_back(*p);
+    e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    return TL_OK;
+}
+
+static void chunk_release(Chunk *c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    mixed_free(c);
+    for (cudaGraphExec_t g : c->graphs)
+        if (g) cudaGraphExecDestroy(g);
+    for (void *p : c->allocations) cudaFree(p);
+    for (auto &p : c->ev_pending) c->ev_pool.push_back(p.second);
+    for (auto &p : c->ev_pool) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    if (c->sc_host) cudaFreeHost(c->sc_host);
+    for (int k = 0; k < 2; ++k)
+        if (c->poll_ev[k]) cudaEventDestroy(c->poll_ev[k]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+static int chunk_alloc(const tl_config_t *cfg, Chunk **out) {
+    *out = nullptr;
+    if (cfg->x_cells < 1 || cfg->y_cells < 1 || cfg->halo_depth < 1 || cfg->max_iters < 0) {
+        set_error("invalid grid: x_cells=%d y_cells=%d halo_depth=%d", cfg->x_cells, cfg->y_cells,
+                  cfg->halo_depth);
+        return TL_ERR_ARG;
+    }
+    if ((long long)(cfg->x_cells + 2 * cfg->halo_depth) * (cfg->y_cells + 2 * cfg->halo_depth) >
+        (1LL << 40)) {
+        set_error("grid too large");
+        return TL_ERR_ARG;
+    }
+    cudaError_t e = cudaSetDevice(cfg->cuda_device < 0 ? 0 : cfg->cuda_device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    Chunk *c = new Chunk();  // value-initialised: every scalar member starts at zero
+    c->cfg = *cfg;
+    c->device = cfg->cuda_device < 0 ? 0 : cfg->cuda_device;
+    c->nx = cfg->x_cells;
+    c->ny = cfg->y_cells;
+    c->h = cfg->halo_depth;
+    c->lead = (32 - c->h % 32) % 32;
+    c->pitch = ((c->nx + 2 * c->h + 31) / 32) * 32;
+    c->rows = c->ny + 2 * c->h;
+    c->alloc_elems = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows + 32;
+    c->g.nx = c->nx;
+    c->g.ny = c->ny;
+    c->g.h = c->h;
+    c->g.pitch = c->pitch;
+    c->g.nstrips = (c->ny + kStrip - 1) / kStrip;
+    c->g.tiles_x = (c->nx + kWarpCols - 1) / kWarpCols;
+    c->g.tiles_y = (c->g.nstrips + kBlockWarps - 1) / kBlockWarps;
+    c->g.tiles = c->g.tiles_x * c->g.tiles_y;
+    c->first = true;
+    c->dt = cfg->dtinit;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->grid_red = sms > 0 ? sms * 4 : 512;
+    if (c->grid_red > kMaxRedBlocks) c->grid_red = kMaxRedBlocks;
+
+    int rc;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "cudaStreamCreate");
+        chunk_release(c);
+        return rc;
+    }
+    double **fields[] = {&c->density, &c->energy0, &c->energy1, &c->u,  &c->u0,    &c->p,
+                         &c->r,       &c->w,       &c->z,       &c->mi, &c->kx,    &c->ky,
+                         &c->sd,      &c->rtemp,   &c->utemp,   &c->r_store, &c->cp, &c->bfp,
+                         &c->volume,  &c->un};
+    for (double **f : fields) {
+        void *p;
+        if ((rc = dalloc(c, &p, c->alloc_elems * sizeof(double)))) {
+            chunk_release(c);
+            return rc;
+        }
+        *f = (double *)p + c->lead;
+    }
+    double **mesh[] = {&c->vertexx, &c->vertexy, &c->cellx, &c->celly, &c->celldx, &c->celldy};
+    size_t mlen = (size_t)(c->nx > c->ny ? c->nx : c->ny) + 2 * c->h + 2;
+    for (double **f : mesh) {
+        void *p;
+        if ((rc = dalloc(c, &p, mlen * sizeof(double)))) {
+            chunk_release(c);
+            return rc;
+        }
+        *f = (double *)p;
+    }
+    void *p;
+    if ((rc = dalloc(c, &p, sizeof(double) * kMaxRedBlocks * 4))) { chunk_release(c); return rc; }
+    c->partials = (double *)p;
+    if ((rc = dalloc(c, &p, 256))) { chunk_release(c); return rc; }
+    c->counter = (unsigned int *)p;
+    if ((rc = dalloc(c, &p, sizeof(DevScalars)))) { chunk_release(c); return rc; }
+    c->sc = (DevScalars *)p;
+    size_t nit = (size_t)cfg->max_iters + 4;
+    if ((rc = dalloc(c, &p, nit * sizeof(double)))) { chunk_release(c); return rc; }
+    c->cg_alphas = (double *)p;
+    if ((rc = dalloc(c, &p, nit * sizeof(double)))) { chunk_release(c); return rc; }
+    c->cg_betas = (double *)p;
+    c->n_coefs_cap = (int)(nit > (size_t)cfg->ppcg_inner_steps + 4 ? nit : (size_t)cfg->ppcg_inner_steps + 4);
+    if ((rc = dalloc(c, &p, (size_t)c->n_coefs_cap * sizeof(double)))) { chunk_release(c); return rc; }
+    c->ch_alphas = (double *)p;
+    if ((rc = dalloc(c, &p, (size_t)c->n_coefs_cap * sizeof(double)))) { chunk_release(c); return rc; }
+    c->ch_betas = (double *)p;
+    e = cudaHostAlloc((void **)&c->sc_host, 3 * sizeof(DevScalars), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "cudaHostAlloc");
+        chunk_release(c);
+        return rc;
+    }
+    memset(c->sc_host, 0, 3 * sizeof(DevScalars));
+    c->poll_host = c->sc_host + 1;
+    for (int k = 0; k < 2; ++k) {
+        e = cudaEventCreateWithFlags(&c->poll_ev[k], cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "cudaEventCreate");
+            chunk_release(c);
+            return rc;
+        }
+    }
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        rc = cuda_fail(e, "chunk init");
+        chunk_release(c);
+        return rc;
+    }
+    *out = c;
+    return TL_OK;
+}
+
+int chunk_sync_scalars(Chunk *c) {
+    TL_CUDA(cudaMemcpyAsync(c->sc_host, c->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, c->stream));
+    TL_CUDA(cudaStreamSynchronize(c->stream));
+    return TL_OK;
+}
+
+int chunk_push_scalars(Chunk *c) {
+    TL_CUDA(cudaMemcpyAsync(c->sc, c->sc_host, sizeof(DevScalars), cudaMemcpyHostToDevice, c->stream));
+    return TL_OK;
+}
+
+// initialise_chunk_kernel.cuknl:3-70 on the host (one-dimensional arrays),
+// volume = dx*dy on the device
+int chunk_initialise_mesh(Chunk *c, double xmin, double ymin, double dx, double dy) {
+    const int h = c->h;
+    const int nvx = c->nx + 2 * h + 1, nvy = c->ny + 2 * h + 1;
+    c->h_vertexx.assign(nvx + 1, 0.0);
+    c->h_vertexy.assign(nvy + 1, 0.0);
+    c->h_cellx.assign(nvx, 0.0);
+    c->h_celly.assign(nvy, 0.0);
+    std::vector<double> cdx(nvx, dx), cdy(nvy, dy);
+    for (int col = 0; col < nvx; ++col) {
+        c->h_vertexx[col] = xmin + dx * (double)(col - h);
+        double plus = xmin + dx * (double)(col - h + 1);
+        c->h_cellx[col] = 0.5 * (c->h_vertexx[col] + plus);
+    }
+    for (int row = 0; row < nvy; ++row) {
+        c->h_vertexy[row] = ymin + dy * (double)(row - h);
+        double plus = ymin + dy * (double)(row - h + 1);
+        c->h_celly[row] = 0.5 * (c->h_vertexy[row] + plus);
+    }
+    c->dx = dx;
+    c->dy = dy;
+    TL_CUDA(cudaMemcpyAsync(c->vertexx, c->h_vertexx.data(), nvx * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaMemcpyAsync(c->vertexy, c->h_vertexy.data(), nvy * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaMemcpyAsync(c->cellx, c->h_cellx.data(), nvx * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaMemcpyAsync(c->celly, c->h_celly.data(), nvy * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaMemcpyAsync(c->celldx, cdx.data(), nvx * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaMemcpyAsync(c->celldy, cdy.data(), nvy * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    int rc = launch_fill(c, c->volume, dx * dy);
+    if (rc) return rc;
+    TL_CUDA(cudaStreamSynchronize(c->stream));
+    return TL_OK;
+}
+
+int chunk_update_halo(Chunk *c, const int *fields, int depth) {
+    if (!c->cfg.reflective_boundary) return TL_OK;
+    double *f[7] = {c->density, c->energy0, c->energy1, c->u, c->p, c->sd, c->r};
+    for (int k = 0; k < 7; ++k)
+        if (fields[k]) {
+            int rc = launch_reflect(c, f[k], depth);
+            if (rc) return rc;
+        }
+    return TL_OK;
+}
+
+// tea_leaf_kernel_cuda.cu:89-104, with the buffer sized once for the
+// largest request (the reference sizes it for the first call only)
+int chunk_upload_coefs(Chunk *c, const double *a, const double *b, int n) {
+    if (n < 0) return TL_OK;
+    if (n > c->n_coefs_cap) {
+        double *na = nullptr, *nb = nullptr;
+        TL_CUDA(cudaMalloc((void **)&na, (size_t)n * sizeof(double)));
+        TL_CUDA(cudaMalloc((void **)&nb, (size_t)n * sizeof(double)));
+        c->allocations.push_back(na);
+        c->allocations.push_back(nb);
+        c->ch_alphas = na;
+        c->ch_betas = nb;
+        c->n_coefs_cap = n;
+        // graphs captured the old pointers
+        for (cudaGraphExec_t &g : c->graphs)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+    if (n == 0) return TL_OK;
+    TL_CUDA(cudaMemcpyAsync(c->ch_alphas, a, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaMemcpyAsync(c->ch_betas, b, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaStreamSynchronize(c->stream));
+    return TL_OK;
+}
+
+// ------------------------------------------------------------ profiling
+
+int prof_begin(Chunk *c, const char *name, int *slot) {
+    int kid = -1;
+    for (size_t k = 0; k < c->prof_names.size(); ++k)
+        if (c->prof_names[k] == name || strcmp(c->prof_names[k], name) == 0) {
+            kid = (int)k;
+            break;
+        }
+    if (kid < 0) {
+        kid = (int)c->prof_names.size();
+        c->prof_names.push_back(name);
+        c->prof_launches.push_back(0);
+        c->prof_ms.push_back(0.0);
+    }
+    std::pair<cudaEvent_t, cudaEvent_t> ev;
+    if (!c->ev_pool.empty()) {
+        ev = c->ev_pool.back();
+        c->ev_pool.pop_back();
+    } else {
+        if (cudaEventCreate(&ev.first) != cudaSuccess) return -1;
+        if (cudaEventCreate(&ev.second) != cudaSuccess) return -1;
+    }
+    cudaEventRecord(ev.first, c->stream);
+    c->ev_pending.push_back({kid, ev});
+    *slot = (int)c->ev_pending.size() - 1;
+    return 0;
+}
+
+void prof_end(Chunk *c, int slot) { cudaEventRecord(c->ev_pending[slot].second.second, c->stream); }
+
+int prof_flush(Chunk *c) {
+    if (c->ev_pending.empty()) return TL_OK;
+    TL_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto &p : c->ev_pending) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) {
+            c->prof_ms[p.first] += ms;
+            c->prof_launches[p.first] += 1;
+        }
+        c->ev_pool.push_back(p.second);
+    }
+    c->ev_pending.clear();
+    return TL_OK;
+}
+
+static int field_summary(Chunk *c, double *vol, double *mass, double *ie, double *temp) {
+    int rc = launch_field_summary(c);
+    if (rc) return rc;
+    if ((rc = chunk_sync_scalars(c))) return rc;
+    if (vol) *vol = c->sc_host->sum[0];
+    if (mass) *mass = c->sc_host->sum[1];
+    if (ie) *ie = c->sc_host->sum[2];
+    if (temp) *temp = c->sc_host->sum[3];
+    return TL_OK;
+}
+
+}  // namespace tl
+
+using namespace tl;
+
+struct tl_chunk {
+    Chunk *c;
+};
+
+static tl_chunk g_default = {nullptr};
+
+extern "C" {
+
+const char *tl_last_error(void) { return g_err; }
+void tl_clear_error(void) { g_err[0] = '\0'; }
+const char *tl_version(void) { return "tealeaf_gb300 1.0 (sm_103a)"; }
+
+long long tl_sizeof(int which) {
+    switch (which) {
+    case 0: return (long long)sizeof(tl_config_t);
+    case 1: return (long long)sizeof(tl_solve_info_t);
+    case 2: return (long long)sizeof(tl_step_record_t);
+    case 3: return (long long)sizeof(tl_run_options_t);
+    case 4: return (long long)sizeof(tl_run_result_t);
+    case 5: return (long long)sizeof(tl_state_t);
+    default: return -1;
+    }
+}
+
+int tl_chunk_create(const tl_config_t *cfg, tl_chunk_t **out) {
+    if (!cfg || !out) {
+        set_error("tl_chunk_create: null argument");
+        return TL_ERR_ARG;
+    }
+    Chunk *c;
+    int rc = chunk_alloc(cfg, &c);
+    if (rc) return rc;
+    tl_chunk_t *h = new tl_chunk{c};
+    *out = h;
+    return TL_OK;
+}
+
+int tl_chunk_destroy(tl_chunk_t *ch) {
+    if (!ch) return TL_OK;
+    chunk_release(ch->c);
+    if (ch != &g_default) delete ch;
+    else g_default.c = nullptr;
+    return TL_OK;
+}
+
+tl_chunk_t *tl_default_chunk(void) { return g_default.c ? &g_default : nullptr; }
+
+int tl_start(tl_chunk_t *ch, double *vol, double *mass, double *ie, double *temp) {
+    if (!ch || !ch->c) {
+        set_error("tl_start: no chunk");
+        return TL_ERR_STATE;
+    }
+    Chunk *c = ch->c;
+    const tl_config_t &cf = c->cfg;
+    // initialise_chunk.f90:33-40
+    double dx = (cf.xmax - cf.xmin) / (double)(float)cf.x_cells;
+    double dy = (cf.ymax - cf.ymin) / (double)(float)cf.y_cells;
+    int rc = chunk_initialise_mesh(c, cf.xmin, cf.ymin, dx, dy);
+    if (rc) return rc;
+    // generate_chunk.f90 / generate_chunk_kernel_cuda.cu:50-110
+    tl_state_t *sdev = nullptr;
+    TL_CUDA(cudaMalloc((void **)&sdev, sizeof(tl_state_t) * (cf.nstates > 0 ? cf.nstates : 1)));
+    cudaMemcpyAsync(sdev, cf.states, sizeof(tl_state_t) * cf.nstates, cudaMemcpyHostToDevice, c->stream);
+    rc = launch_generate(c, cf.nstates, sdev);
+    cudaStreamSynchronize(c->stream);
+    cudaFree(sdev);
+    if (rc) return rc;
+    // start.f90:88-105: halo of density/energy, then energy1 = energy0
+    int fl[7] = {1, 1, 1, 0, 0, 0, 0};
+    if ((rc = chunk_update_halo(c, fl, c->h))) return rc;
+    if ((rc = launch_set_field(c))) return rc;
+    c->dt = cf.dtinit;
+    return field_summary(c, vol, mass, ie, temp);
+}
+
+int tl_timestep(tl_chunk_t *ch, tl_solve_info_t *info) {
+    if (!ch || !ch->c || !info) {
+        set_error("tl_timestep: no chunk");
+        return TL_ERR_STATE;
+    }
+    if (ch->c->cfg.precision == TL_PRECISION_MIXED) return solve_timestep_mixed(ch->c, info);
+    return solve_timestep(ch->c, info);
+}
+
+int tl_field_summary(tl_chunk_t *ch, double *vol, double *mass, double *ie, double *temp) {
+    if (!ch || !ch->c) {
+        set_error("tl_field_summary: no chunk");
+        return TL_ERR_STATE;
+    }
+    return field_summary(ch->c, vol, mass, ie, temp);
+}
+
+int tl_get_field(tl_chunk_t *ch, int field, double *host) {
+    if (!ch || !ch->c || !host) {
+        set_error("tl_get_field: bad argument");
+        return TL_ERR_ARG;
+    }
+    Chunk *c = ch->c;
+    double *f = field_ptr(c, field);
+    if (!f) {
+        set_error("tl_get_field: unknown field %d", field);
+        return TL_ERR_ARG;
+    }
+    const size_t w = (size_t)(c->nx + 2 * c->h);
+    TL_CUDA(cudaMemcpy2DAsync(host, w * sizeof(double), f, (size_t)c->pitch * sizeof(double),
+                              w * sizeof(double), (size_t)c->rows, cudaMemcpyDeviceToHost, c->stream));
+    TL_CUDA(cudaStreamSynchronize(c->stream));
+    return TL_OK;
+}
+
+int tl_set_field(tl_chunk_t *ch, int field, const double *host) {
+    if (!ch || !ch->c || !host) {
+        set_error("tl_set_field: bad argument");
+        return TL_ERR_ARG;
+    }
+    Chunk *c = ch->c;
+    double *f = field_ptr(c, field);
+    if (!f) {
+        set_error("tl_set_field: unknown field %d", field);
+        return TL_ERR_ARG;
+    }
+    const size_t w = (size_t)(c->nx + 2 * c->h);
+    TL_CUDA(cudaMemcpy2DAsync(f, (size_t)c->pitch * sizeof(double), host, w * sizeof(double),
+                              w * sizeof(double), (size_t)c->rows, cudaMemcpyHostToDevice, c->stream));
+    TL_CUDA(cudaStreamSynchronize(c->stream));
+    return TL_OK;
+}
+
+int tl_set_dt(tl_chunk_t *ch, double dt) {
+    if (!ch || !ch->c) {
+        set_error("tl_set_dt: no chunk");
+        return TL_ERR_STATE;
+    }
+    ch->c->dt = dt;
+    return TL_OK;
+}
+
+long long tl_kernel_launches(tl_chunk_t *ch) { return (ch && ch->c) ? ch->c->launches : 0; }
+
+void *tl_chunk_stream(tl_chunk_t *ch) { return (ch && ch->c) ? (void *)ch->c->stream : nullptr; }
+
+int tl_set_profiling(tl_chunk_t *ch, int on) {
+    if (!ch || !ch->c) {
+        set_error("tl_set_profiling: no chunk");
+        return TL_ERR_STATE;
+    }
+    int rc = prof_flush(ch->c);
+    ch->c->profiling = on != 0;
+    return rc;
+}
+
+int tl_profile_reset(tl_chunk_t *ch) {
+    if (!ch || !ch->c) return TL_ERR_STATE;
+    int rc = prof_flush(ch->c);
+    for (auto &v : ch->c->prof_ms) v = 0.0;
+    for (auto &v : ch->c->prof_launches) v = 0;
+    return rc;
+}
+
+int tl_profile_read(tl_chunk_t *ch, int idx, const char **name, long long *launches, double *ms) {
+    if (!ch || !ch->c) return TL_ERR_STATE;
+    Chunk *c = ch->c;
+    int rc = prof_flush(c);
+    if (rc) return rc;
+    if (idx < 0 || idx >= (int)c->prof_names.size()) return TL_ERR_ARG;
+    if (name) *name = c->prof_names[idx];
+    if (launches) *launches = c->prof_launches[idx];
+    if (ms) *ms = c->prof_ms[idx];
+    return TL_OK;
+}
+
+}  // extern "C"
+
+// the process-wide chunk of the reference-named entry points
+namespace tl {
+int default_chunk_replace(const tl_config_t *cfg);
+}
+extern "C" int tl_default_chunk_init(const tl_config_t *cfg) {
+    if (!cfg) {
+        set_error("tl_default_chunk_init: null config");
+        return TL_ERR_ARG;
+    }
+    return tl::default_chunk_replace(cfg);
+}
+namespace tl {
+int default_chunk_replace(const tl_config_t *cfg) {
+    if (g_default.c) {
+        chunk_release(g_default.c);
+        g_default.c = nullptr;
+    }
+    Chunk *c;
+    int rc = chunk_alloc(cfg, &c);
+    if (rc) return rc;
+    g_default.c = c;
+    return TL_OK;
+}
+Chunk *default_chunk() { return g_default.c; }
+}  // namespace tl
