@@ -52,6 +52,7 @@
 #endif
 
 #define G_SMALL 1.0e-16 /* data.f90:30 */
+#define ORA_PAR_MIN 65536 /* grids smaller than this run on one thread */
 
 struct ora_chunk {
     ora_config cfg;
@@ -555,7 +556,7 @@ static void initialise_chunk(ora_chunk *ch) {
 static void generate_chunk(ora_chunk *ch) {
     const ora_config *c = &ch->cfg;
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -564,7 +565,7 @@ static void generate_chunk(ora_chunk *ch) {
         }
     for (int s = 1; s < c->nstates; ++s) {
         const ora_state *st = &c->states[s];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
         for (int row = h; row < h + ch->ny; ++row)
             for (int col = h; col < h + ch->nx; ++col) {
                 size_t i = IDX(ch, col, row);
@@ -587,7 +588,7 @@ static void generate_chunk(ora_chunk *ch) {
             }
     }
     /* generate_chunk_init_u(energy0): u = u0 = energy*density */
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -644,7 +645,7 @@ void ora_field_summary(ora_chunk *ch, double *vol, double *mass, double *ie, dou
     int h = ch->h;
     double *rb[4];
     for (int k = 0; k < 4; ++k) rb[k] = zalloc((size_t)ch->rows);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row) {
         double v = 0, m = 0, e = 0, t = 0;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -684,7 +685,7 @@ void ora_common_init(ora_chunk *ch, double dt, double *rx_out, double *ry_out) {
     const size_t P = (size_t)ch->pitch;
     /* device_tea_leaf_init_common over columns h..nx+2h-1, rows h..ny+2h-1
      * (tea_leaf_common.cuknl:60-97, range init_cuda.cu:290) */
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < ny + 2 * h; ++row)
         for (int col = h; col < nx + 2 * h; ++col) {
             size_t i = IDX(ch, col, row);
@@ -715,7 +716,7 @@ void ora_common_init(ora_chunk *ch, double dt, double *rx_out, double *ry_out) {
             }
     }
     /* generate_chunk_init_u(energy1) */
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ny; ++row)
         for (int col = h; col < h + nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -727,7 +728,7 @@ void ora_common_init(ora_chunk *ch, double dt, double *rx_out, double *ry_out) {
 /* tea_leaf_common.cuknl:19-39 */
 void ora_calc_residual(ora_chunk *ch) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -737,7 +738,7 @@ void ora_calc_residual(ora_chunk *ch) {
 
 static double dot(ora_chunk *ch, const double *a, const double *b) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row) {
         double s = 0.0;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -765,7 +766,7 @@ double ora_calc_2norm(ora_chunk *ch, int norm_array) {
 static void block_init(ora_chunk *ch) {
     int h = ch->h, ny = ch->ny;
     const size_t P = (size_t)ch->pitch;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int s0 = 0; s0 < ny; s0 += STRIP) {
         int m = ny - s0 < STRIP ? ny - s0 : STRIP;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -802,7 +803,7 @@ static inline void strip_solve(const ora_chunk *ch, size_t i0, int m, const doub
 static void block_solve(ora_chunk *ch, const double *src, double *dst) {
     int h = ch->h, ny = ch->ny;
     const size_t P = (size_t)ch->pitch;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int s0 = 0; s0 < ny; s0 += STRIP) {
         int m = ny - s0 < STRIP ? ny - s0 : STRIP;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -818,7 +819,7 @@ static void block_solve(ora_chunk *ch, const double *src, double *dst) {
 /* tea_leaf_common.cuknl:131-147 */
 static void init_jac_diag(ora_chunk *ch) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -835,7 +836,7 @@ double ora_cg_init(ora_chunk *ch) {
     } else if (pc == ORA_PREC_DIAG) {
         init_jac_diag(ch);
     }
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row) {
         double s = 0.0;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -858,7 +859,7 @@ double ora_cg_init(ora_chunk *ch) {
 /* tea_leaf_cg.cuknl:43-68 */
 double ora_cg_calc_w(ora_chunk *ch) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row) {
         double s = 0.0;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -874,7 +875,7 @@ double ora_cg_calc_w(ora_chunk *ch) {
 /* tea_leaf_cg.cuknl:72-137 */
 double ora_cg_calc_ur(ora_chunk *ch, double alpha) {
     int h = ch->h, pc = ch->cfg.precond;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -886,7 +887,7 @@ double ora_cg_calc_ur(ora_chunk *ch, double alpha) {
         return dot(ch, ch->r, ch->z);
     }
     if (pc == ORA_PREC_DIAG) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
         for (int row = h; row < h + ch->ny; ++row) {
             double s = 0.0;
             for (int col = h; col < h + ch->nx; ++col) {
@@ -905,7 +906,7 @@ double ora_cg_calc_ur(ora_chunk *ch, double alpha) {
 void ora_cg_calc_p(ora_chunk *ch, double beta) {
     int h = ch->h;
     const double *src = ch->cfg.precond != ORA_PREC_NONE ? ch->z : ch->r;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -925,7 +926,7 @@ static void upload_coefs(ora_chunk *ch, const double *a, const double *b, int n)
 void ora_cheby_init(ora_chunk *ch, const double *alphas, const double *betas, int n, double theta) {
     int h = ch->h, pc = ch->cfg.precond;
     upload_coefs(ch, alphas, betas, n);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -933,7 +934,7 @@ void ora_cheby_init(ora_chunk *ch, const double *alphas, const double *betas, in
             ch->r[i] = ch->u0[i] - ch->w[i];
         }
     if (pc == ORA_PREC_BLOCK) block_solve(ch, ch->r, ch->un);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -949,7 +950,7 @@ void ora_cheby_init(ora_chunk *ch, const double *alphas, const double *betas, in
 void ora_cheby_iterate(ora_chunk *ch, int step) {
     int h = ch->h, pc = ch->cfg.precond;
     double al = ch->ch_alphas_dev[step - 1], be = ch->ch_betas_dev[step - 1];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -957,7 +958,7 @@ void ora_cheby_iterate(ora_chunk *ch, int step) {
             ch->r[i] = ch->u0[i] - ch->w[i];
         }
     if (pc == ORA_PREC_BLOCK) block_solve(ch, ch->r, ch->un);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -977,7 +978,7 @@ void ora_ppcg_init_constants(ora_chunk *ch, const double *alphas, const double *
  * Steps 1 and 3 return sum r.p, step 2 returns 0. */
 double ora_ppcg_init(ora_chunk *ch, int step) {
     int h = ch->h, pc = ch->cfg.precond;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -993,7 +994,7 @@ double ora_ppcg_init(ora_chunk *ch, int step) {
             if (pc == ORA_PREC_BLOCK) {
                 block_solve(ch, ch->r, ch->z);
             } else if (pc == ORA_PREC_DIAG) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
                 for (int row = h; row < h + ch->ny; ++row)
                     for (int col = h; col < h + ch->nx; ++col) {
                         size_t i = IDX(ch, col, row);
@@ -1002,7 +1003,7 @@ double ora_ppcg_init(ora_chunk *ch, int step) {
             }
         }
         if (step == 1 || step == 3) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
             for (int row = h; row < h + ch->ny; ++row)
                 for (int col = h; col < h + ch->nx; ++col) {
                     size_t i = IDX(ch, col, row);
@@ -1010,7 +1011,7 @@ double ora_ppcg_init(ora_chunk *ch, int step) {
                 }
         }
     } else if (step == 1) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
         for (int row = h; row < h + ch->ny; ++row)
             for (int col = h; col < h + ch->nx; ++col) {
                 size_t i = IDX(ch, col, row);
@@ -1026,7 +1027,7 @@ void ora_ppcg_init_sd_new(ora_chunk *ch, double theta) {
     int h = ch->h, pc = ch->cfg.precond;
     double theta_r = 1.0 / theta;
     const double *src = pc != ORA_PREC_NONE ? ch->z : ch->r;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -1041,14 +1042,14 @@ void ora_ppcg_init_sd_new(ora_chunk *ch, double theta) {
 void ora_ppcg_inner(ora_chunk *ch, int step) {
     int h = ch->h, pc = ch->cfg.precond;
     double al = ch->ch_alphas_dev[step - 1], be = ch->ch_betas_dev[step - 1];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
             ch->rtemp[i] -= smvp(ch, ch->sd, i);
         }
     if (pc == ORA_PREC_BLOCK) block_solve(ch, ch->rtemp, ch->un);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -1080,7 +1081,7 @@ void ora_ppcg_update_z(ora_chunk *ch) {
 /* tea_leaf_ppcg.cuknl:279-297: sum (r - r_store) * z */
 double ora_ppcg_calc_rrn(ora_chunk *ch) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row) {
         double s = 0.0;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -1098,7 +1099,7 @@ double ora_ppcg_calc_zrnorm(ora_chunk *ch) { return dot(ch, ch->r, ch->z); }
 /* tea_leaf_ppcg.cuknl:301-313 */
 void ora_ppcg_calc_p(ora_chunk *ch, double beta) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
@@ -1111,7 +1112,7 @@ double ora_jacobi_solve(ora_chunk *ch) {
     int h = ch->h;
     const size_t P = (size_t)ch->pitch;
     memcpy(ch->un, ch->u, ch->n2d * sizeof(double));
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row) {
         double s = 0.0;
         for (int col = h; col < h + ch->nx; ++col) {
@@ -1133,7 +1134,7 @@ double ora_jacobi_solve(ora_chunk *ch) {
 /* tea_leaf_common.cuknl:5-17 */
 void ora_finalise(ora_chunk *ch) {
     int h = ch->h;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) if (ch->nx * ch->ny >= ORA_PAR_MIN)
     for (int row = h; row < h + ch->ny; ++row)
         for (int col = h; col < h + ch->nx; ++col) {
             size_t i = IDX(ch, col, row);
