@@ -181,6 +181,25 @@ tl_chunk_t *tl_default_chunk(void);
  * the same from ./tea.in) */
 int tl_default_chunk_init(const tl_config_t *cfg);
 
+/* tl_dot_noalloc -- no counterpart in the reference.  The dot-product
+ * reduction of tea_leaf_calc_2norm (sum of a[i]*b[i]) for callers that
+ * cannot let the library allocate: hosts that set up their whole
+ * device-memory budget once and then run under a fixed cap, hosts whose
+ * device memory belongs to another allocator, and hosts that cannot take the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  a and b are device
+ * pointers to the first element of an nx-by-ny block whose rows are `pitch`
+ * elements apart; the sum is written to the device double *result on
+ * `stream` (a cudaStream_t, NULL for the default stream), asynchronously.
+ * The call allocates nothing: its scratch is a fixed 1 MiB device array
+ * held by every GPU that loads the library until the process exits (one
+ * partial sum per 32x32 tile, so at most 131040 tiles, about 134 million
+ * cells; larger blocks are rejected with TL_ERR_ARG).  The first call on a
+ * device looks up that array's address with the device current; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race on it and must be ordered by the caller. */
+int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long pitch,
+                   double *result, void *stream);
+
 /* ------------------------------------------------------- whole program
  * The main program of the reference (tea_leaf.f90 -> start.f90 ->
  * diffuse.f90) restated in C++: read a deck, set up the chunk, run the

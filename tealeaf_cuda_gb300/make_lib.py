@@ -22,7 +22,8 @@ EXE = os.path.join(OUT, "tea_leaf")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["tl_kernels.cu", "tl_chunk.cu", "tl_solve.cu", "tl_legacy.cu", "tl_mixed.cu"]
+CU_SOURCES = ["tl_kernels.cu", "tl_chunk.cu", "tl_solve.cu", "tl_legacy.cu", "tl_mixed.cu",
+              "tl_noalloc.cu"]
 CPP_SOURCES = ["tl_deck.cpp", "tl_driver.cpp", "tl_host_numerics.cpp"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]
