@@ -63,8 +63,16 @@ BYTES_PER_CELL = {
     "residual": 40,      # read u, u0, Kx, Ky; write r
     "cg_init": 48,       # read r, Kx, Ky; write Mi, z, p
     "common_init": 56,   # read density, energy; write Kx, Ky, u, u0
+    "diag": 24,          # read Kx, Ky; write diag
     "field_summary": 32,
     "finalise": 24,
+    # mixed precision: FP32 inner iteration (4-byte elements)
+    "mixed_w": 16,       # read p, Kx, Ky; write w
+    "mixed_ur": 32,      # jac_diag: read d, p, r, w, Mi; write d, r, z
+    "mixed_p": 12,       # read z, p; write p
+    "mixed_init": 28,    # read r (FP64), Mi; write r, z, p, d
+    "mixed_update_u": 20,  # read u (FP64), d; write u (FP64)
+    "mixed_convert": 40,   # read Kx, Ky (FP64); write Kx, Ky, Mi (FP32)
 }
 
 

@@ -132,7 +132,7 @@ static int chunk_alloc(const tl_config_t *cfg, Chunk **out) {
     double **fields[] = {&c->density, &c->energy0, &c->energy1, &c->u,  &c->u0,    &c->p,
                          &c->r,       &c->w,       &c->z,       &c->mi, &c->kx,    &c->ky,
                          &c->sd,      &c->rtemp,   &c->utemp,   &c->r_store, &c->cp, &c->bfp,
-                         &c->volume,  &c->un};
+                         &c->volume,  &c->un,    &c->diag};
     for (double **f : fields) {
         void *p;
         if ((rc = dalloc(c, &p, c->alloc_elems * sizeof(double)))) {

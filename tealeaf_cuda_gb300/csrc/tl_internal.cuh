@@ -33,6 +33,9 @@ struct DevScalars {
     double sum[4];                 // generic reduction outputs
     double inner_rr;               // mixed-precision inner scalars
     double theta;                  // Chebyshev / PPCG centre of the spectrum
+    // inner FP32 Krylov solve of the mixed form (its scalars stay FP64)
+    double in_rro, in_pw, in_rrn, in_alpha, in_beta, in_target;
+    int in_n, in_max;
     int n;                         // current iteration (1-based)
     int max_iters;
     int done;                      // 0 running, 1 converged, 2 max_iters, 3 switch, 4 breakdown
@@ -95,6 +98,7 @@ struct Chunk {
     // fields (padded reference coordinates)
     double *density, *energy0, *energy1, *u, *u0, *p, *r, *w, *z, *mi, *kx, *ky, *sd,
         *rtemp, *utemp, *r_store, *cp, *bfp, *volume, *un;
+    double *diag;                // diag(A), refreshed with Kx/Ky by common_init
     std::vector<void *> allocations;
     // mesh
     double *vertexx, *vertexy, *cellx, *celly, *celldx, *celldy;
@@ -114,8 +118,8 @@ struct Chunk {
     bool first;
     double eigmin, eigmax, theta, cn;
     // graphs of the device-resident loop
-    cudaGraphExec_t graphs[4];   // CG, PPCG, Chebyshev, Jacobi phases
-    long long graph_kernels[4];
+    cudaGraphExec_t graphs[6];   // CG, PPCG, Chebyshev, Jacobi, mixed inner
+    long long graph_kernels[6];
     long long launches;
     int grid_red;                // CTAs of the grid-stride kernels
     // mixed precision state (allocated on first use)
@@ -198,6 +202,10 @@ int chunk_initialise_mesh(Chunk *c, double xmin, double ymin, double dx, double 
 int chunk_update_halo(Chunk *c, const int *fields, int depth);
 int chunk_upload_coefs(Chunk *c, const double *a, const double *b, int n);
 int solve_timestep(Chunk *c, tl_solve_info_t *info);       // tl_solve.cu
+// run `iters`-iteration graphs of `body` (graph slot `phase`) until the
+// device sets DevScalars::done; *done_out receives it (tl_solve.cu)
+int run_phase(Chunk *c, int (*body)(Chunk *), int iters, int phase, int *done_out);
+constexpr int kPhaseMixedInner = 4;
 int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
 

@@ -205,7 +205,8 @@ __device__ __forceinline__ double diag_at(const double *__restrict__ kx,
 // the centre values.  Rows beyond m are neither read nor written.
 template <class X>
 __device__ __forceinline__ void strip_apply(const double *__restrict__ kx,
-                                            const double *__restrict__ ky, int pitch,
+                                            const double *__restrict__ ky,
+                                            const double *__restrict__ dg, int pitch,
                                             int64_t base, int m, X x, double (&xc)[4],
                                             double (&ax)[4]) {
     double xr[6];   // rows -1..4
@@ -222,7 +223,7 @@ __device__ __forceinline__ void strip_apply(const double *__restrict__ kx,
             const int64_t i = base + (int64_t)k * pitch;
             const double kxc = kx[i], kxe = kx[i + 1];
             const double xw = x(i - 1), xe = x(i + 1);
-            const double diag = (1.0 + (kyr[k + 1] + kyr[k])) + (kxe + kxc);
+            const double diag = dg[i];
             const double a = fma(kyr[k + 1], xr[k + 2], kyr[k] * xr[k]);
             const double b = fma(kxe, xe, kxc * xw);
             ax[k] = fma(diag, xr[k + 1], -a) - b;
@@ -232,14 +233,14 @@ __device__ __forceinline__ void strip_apply(const double *__restrict__ kx,
 }
 
 // block-Jacobi strip solve z = M^-1 x (tea_block_jacobi.cuknl:11-46)
-__device__ __forceinline__ void strip_block_solve(const double *__restrict__ kx,
+__device__ __forceinline__ void strip_block_solve(const double *__restrict__ dg,
                                                   const double *__restrict__ ky,
                                                   const double *__restrict__ cp,
                                                   const double *__restrict__ bfp, int pitch,
                                                   int64_t base, int m, const double (&x)[4],
                                                   double (&z)[4]) {
     double dp[4];
-    dp[0] = x[0] / diag_at(kx, ky, base, pitch);
+    dp[0] = x[0] / dg[base];
 #pragma unroll
     for (int k = 1; k < 4; ++k)
         if (k < m) {
@@ -267,13 +268,14 @@ __device__ __forceinline__ double coef(const double *p, double v) { return p ? *
 // ------------------------------------------------------------- bodies
 
 struct BodyResidual {  // r = u0 - A u  (+ r.r)
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *u, *u0, *kx, *ky;
     double *r;
     int pitch;
     __device__ void setup() {}
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
         double xc[4], ax[4];
-        strip_apply(kx, ky, pitch, base, m, LoadX{u}, xc, ax);
+        strip_apply(kx, ky, dg, pitch, base, m, LoadX{u}, xc, ax);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -301,6 +303,7 @@ struct BodyNorm {  // sum a.b
 
 template <int PC>
 struct BodyCgInit {  // tea_leaf_kernel_cuda.cu:164-186 fused per strip
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *r, *kx, *ky;
     double *p, *z, *mi, *cp, *bfp;
     int pitch;
@@ -312,18 +315,18 @@ struct BodyCgInit {  // tea_leaf_kernel_cuda.cu:164-186 fused per strip
             if (k < m) rv[k] = r[base + (int64_t)k * pitch];
         if (PC == TL_PREC_JAC_BLOCK) {
             // block_init (tea_block_jacobi.cuknl:83-111)
-            double cprev = (-ky[base + pitch]) / diag_at(kx, ky, base, pitch);
+            double cprev = (-ky[base + pitch]) / dg[base];
             cp[base] = cprev;
 #pragma unroll
             for (int k = 1; k < 4; ++k)
                 if (k < m) {
                     const int64_t i = base + (int64_t)k * pitch;
-                    const double bf = 1.0 / fma(ky[i], cprev, diag_at(kx, ky, i, pitch));
+                    const double bf = 1.0 / fma(ky[i], cprev, dg[i]);
                     bfp[i] = bf;
                     cprev = (-ky[i + pitch]) * bf;
                     cp[i] = cprev;
                 }
-            strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+            strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k)
@@ -334,7 +337,7 @@ struct BodyCgInit {  // tea_leaf_kernel_cuda.cu:164-186 fused per strip
                     z[i] = zv[k];
                     pv = zv[k];
                 } else if (PC == TL_PREC_JAC_DIAG) {
-                    const double mv = 1.0 / diag_at(kx, ky, i, pitch);
+                    const double mv = 1.0 / dg[i];
                     mi[i] = mv;
                     const double zz = rv[k] * mv;
                     z[i] = zz;
@@ -349,13 +352,14 @@ struct BodyCgInit {  // tea_leaf_kernel_cuda.cu:164-186 fused per strip
 };
 
 struct BodyCgW {  // w = A p; p.w  (tea_leaf_cg.cuknl:43-68)
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *p, *kx, *ky;
     double *w;
     int pitch;
     __device__ void setup() {}
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
         double xc[4], ax[4];
-        strip_apply(kx, ky, pitch, base, m, LoadX{p}, xc, ax);
+        strip_apply(kx, ky, dg, pitch, base, m, LoadX{p}, xc, ax);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -367,6 +371,7 @@ struct BodyCgW {  // w = A p; p.w  (tea_leaf_cg.cuknl:43-68)
 
 template <int PC>
 struct BodyCgUr {  // tea_leaf_cg.cuknl:72-137
+    const double *dg;  // diag(A), stored by the diag kernel
     double *u, *r, *z;
     const double *p, *w, *mi, *kx, *ky, *cp, *bfp;
     const double *alpha_p;
@@ -386,7 +391,7 @@ struct BodyCgUr {  // tea_leaf_cg.cuknl:72-137
             }
         if (PC == TL_PREC_JAC_BLOCK) {
             double zv[4];
-            strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+            strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 if (k < m) {
@@ -430,6 +435,7 @@ struct BodyAxpyP {  // p = src + beta p  (tea_leaf_cg.cuknl:141-161, tea_leaf_pp
 
 template <int PC>
 struct BodyChebyInitP {  // tea_leaf_cheby.cuknl:5-68
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *u, *u0, *kx, *ky, *mi, *cp, *bfp;
     double *p, *r, *w;
     double theta;
@@ -437,7 +443,7 @@ struct BodyChebyInitP {  // tea_leaf_cheby.cuknl:5-68
     __device__ void setup() {}
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
         double xc[4], ax[4], rv[4], zv[4];
-        strip_apply(kx, ky, pitch, base, m, LoadX{u}, xc, ax);
+        strip_apply(kx, ky, dg, pitch, base, m, LoadX{u}, xc, ax);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -446,7 +452,7 @@ struct BodyChebyInitP {  // tea_leaf_cheby.cuknl:5-68
                 rv[k] = u0[i] - ax[k];
                 r[i] = rv[k];
             }
-        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -460,6 +466,7 @@ struct BodyChebyInitP {  // tea_leaf_cheby.cuknl:5-68
 
 template <int PC>
 struct BodyChebyCalcP {  // tea_leaf_cheby.cuknl:84-152 (+ r.r for the exit test)
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *u, *u0, *kx, *ky, *mi, *cp, *bfp, *alphas, *betas;
     double *p, *r, *w;
     const int *step_p;   // device cheby_calc_steps, or nullptr
@@ -473,7 +480,7 @@ struct BodyChebyCalcP {  // tea_leaf_cheby.cuknl:84-152 (+ r.r for the exit test
     }
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
         double xc[4], ax[4], rv[4], zv[4];
-        strip_apply(kx, ky, pitch, base, m, LoadX{u}, xc, ax);
+        strip_apply(kx, ky, dg, pitch, base, m, LoadX{u}, xc, ax);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -483,7 +490,7 @@ struct BodyChebyCalcP {  // tea_leaf_cheby.cuknl:84-152 (+ r.r for the exit test
                 r[i] = rv[k];
                 acc[0] = fma(rv[k], rv[k], acc[0]);
             }
-        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -512,6 +519,7 @@ struct BodyAdd {  // u += p  (tea_leaf_cheby.cuknl:71-82)
 
 template <int PC>
 struct BodyPpcgInit {  // tea_leaf_ppcg.cuknl:319-420
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *r, *mi, *kx, *ky, *cp, *bfp;
     double *p, *z;
     int step, pitch;
@@ -522,7 +530,7 @@ struct BodyPpcgInit {  // tea_leaf_ppcg.cuknl:319-420
         for (int k = 0; k < 4; ++k)
             if (k < m) rv[k] = r[base + (int64_t)k * pitch];
         const bool do_z = (PC != TL_PREC_NONE || step == 3) && (step == 1 || step == 2);
-        if (do_z && PC == TL_PREC_JAC_BLOCK) strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+        if (do_z && PC == TL_PREC_JAC_BLOCK) strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -550,6 +558,7 @@ struct BodyPpcgInit {  // tea_leaf_ppcg.cuknl:319-420
 
 template <int PC>
 struct BodyPpcgInitSd {  // tea_leaf_ppcg.cuknl:5-55 (not used by the driver)
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *r, *mi, *kx, *ky, *cp, *bfp;
     double *sd;
     double theta;
@@ -560,7 +569,7 @@ struct BodyPpcgInitSd {  // tea_leaf_ppcg.cuknl:5-55 (not used by the driver)
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) rv[k] = r[base + (int64_t)k * pitch];
-        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -596,13 +605,14 @@ struct BodyPpcgInitSdNew {  // tea_leaf_ppcg.cuknl:58-89
 };
 
 struct BodyPpcgUpdateR {  // rtemp -= A sd  (tea_leaf_ppcg.cuknl:154-173)
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *sd, *kx, *ky;
     double *rtemp;
     int pitch;
     __device__ void setup() {}
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
         double xc[4], ax[4];
-        strip_apply(kx, ky, pitch, base, m, LoadX{sd}, xc, ax);
+        strip_apply(kx, ky, dg, pitch, base, m, LoadX{sd}, xc, ax);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -614,6 +624,7 @@ struct BodyPpcgUpdateR {  // rtemp -= A sd  (tea_leaf_ppcg.cuknl:154-173)
 
 template <int PC>
 struct BodyPpcgCalcSdNew {  // tea_leaf_ppcg.cuknl:178-244
+    const double *dg;  // diag(A), stored by the diag kernel
     const double *rtemp, *mi, *kx, *ky, *cp, *bfp, *alphas, *betas;
     double *sd, *utemp;
     int step;  // 1-based inner step
@@ -628,7 +639,7 @@ struct BodyPpcgCalcSdNew {  // tea_leaf_ppcg.cuknl:178-244
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) rv[k] = rtemp[base + (int64_t)k * pitch];
-        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(kx, ky, cp, bfp, pitch, base, m, rv, zv);
+        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -724,6 +735,21 @@ struct BodyFieldSummary {  // field_summary_kernel.cuknl:5-58
                 acc[1] += cm;
                 acc[2] += cm * energy1[i];
                 acc[3] += cm * u[i];
+            }
+    }
+};
+
+struct BodyDiag {  // diag(A) of tea_leaf_common.cuknl:137-139, once per solve
+    const double *kx, *ky;
+    double *dg;
+    int pitch;
+    __device__ void setup() {}
+    __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = base + (int64_t)k * pitch;
+                dg[i] = diag_at(kx, ky, i, pitch);
             }
     }
 };
@@ -869,11 +895,12 @@ int launch_common_init(Chunk *c, int coefficient, double rx, double ry, const in
     c->launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "common_init launch");
-    return TL_OK;
+    BodyDiag bd{c->kx, c->ky, c->diag, c->pitch};
+    return run<1>(c, "diag", bd, kEpiNone, false);
 }
 
 int launch_residual(Chunk *c, int epi) {
-    BodyResidual b{c->u, c->u0, c->kx, c->ky, c->r, c->pitch};
+    BodyResidual b{c->diag, c->u, c->u0, c->kx, c->ky, c->r, c->pitch};
     return run<1>(c, "residual", b, epi, false);
 }
 
@@ -885,28 +912,28 @@ int launch_norm(Chunk *c, const double *a, const double *bb, int epi) {
 int launch_cg_init(Chunk *c, int epi) {
     switch (c->cfg.precond) {
     case TL_PREC_JAC_BLOCK: {
-        BodyCgInit<TL_PREC_JAC_BLOCK> b{c->r, c->kx, c->ky, c->p, c->z, c->mi, c->cp, c->bfp, c->pitch};
+        BodyCgInit<TL_PREC_JAC_BLOCK> b{c->diag, c->r, c->kx, c->ky, c->p, c->z, c->mi, c->cp, c->bfp, c->pitch};
         return run<1>(c, "cg_init", b, epi, false);
     }
     case TL_PREC_JAC_DIAG: {
-        BodyCgInit<TL_PREC_JAC_DIAG> b{c->r, c->kx, c->ky, c->p, c->z, c->mi, c->cp, c->bfp, c->pitch};
+        BodyCgInit<TL_PREC_JAC_DIAG> b{c->diag, c->r, c->kx, c->ky, c->p, c->z, c->mi, c->cp, c->bfp, c->pitch};
         return run<1>(c, "cg_init", b, epi, false);
     }
     default: {
-        BodyCgInit<TL_PREC_NONE> b{c->r, c->kx, c->ky, c->p, c->z, c->mi, c->cp, c->bfp, c->pitch};
+        BodyCgInit<TL_PREC_NONE> b{c->diag, c->r, c->kx, c->ky, c->p, c->z, c->mi, c->cp, c->bfp, c->pitch};
         return run<1>(c, "cg_init", b, epi, false);
     }
     }
 }
 
 int launch_cg_w(Chunk *c, int epi, bool fast) {
-    BodyCgW b{c->p, c->kx, c->ky, c->w, c->pitch};
+    BodyCgW b{c->diag, c->p, c->kx, c->ky, c->w, c->pitch};
     return run<1>(c, "cg_w", b, epi, fast);
 }
 
 template <int PC>
 static int cg_ur(Chunk *c, double alpha, int epi, bool fast) {
-    BodyCgUr<PC> b{c->u, c->r, c->z, c->p, c->w, c->mi, c->kx, c->ky, c->cp, c->bfp,
+    BodyCgUr<PC> b{c->diag, c->u, c->r, c->z, c->p, c->w, c->mi, c->kx, c->ky, c->cp, c->bfp,
                    fast ? &c->sc->alpha : nullptr, alpha, c->pitch, 0.0};
     return run<1>(c, "cg_ur", b, epi, fast);
 }
@@ -928,17 +955,17 @@ int launch_cg_p(Chunk *c, double beta, int epi, bool fast) {
 int launch_cheby_init(Chunk *c, double theta) {
     switch (c->cfg.precond) {
     case TL_PREC_JAC_BLOCK: {
-        BodyChebyInitP<TL_PREC_JAC_BLOCK> b{c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp,
+        BodyChebyInitP<TL_PREC_JAC_BLOCK> b{c->diag, c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp,
                                             c->p, c->r, c->w, theta, c->pitch};
         return run<1>(c, "cheby_init", b, kEpiNone, false);
     }
     case TL_PREC_JAC_DIAG: {
-        BodyChebyInitP<TL_PREC_JAC_DIAG> b{c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp,
+        BodyChebyInitP<TL_PREC_JAC_DIAG> b{c->diag, c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp,
                                            c->p, c->r, c->w, theta, c->pitch};
         return run<1>(c, "cheby_init", b, kEpiNone, false);
     }
     default: {
-        BodyChebyInitP<TL_PREC_NONE> b{c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp,
+        BodyChebyInitP<TL_PREC_NONE> b{c->diag, c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp,
                                        c->p, c->r, c->w, theta, c->pitch};
         return run<1>(c, "cheby_init", b, kEpiNone, false);
     }
@@ -947,7 +974,7 @@ int launch_cheby_init(Chunk *c, double theta) {
 
 template <int PC>
 static int cheby_p(Chunk *c, int step, int epi, bool fast) {
-    BodyChebyCalcP<PC> b{c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp, c->ch_alphas,
+    BodyChebyCalcP<PC> b{c->diag, c->u, c->u0, c->kx, c->ky, c->mi, c->cp, c->bfp, c->ch_alphas,
                          c->ch_betas, c->p, c->r, c->w,
                          fast ? &c->sc->cheby_calc_steps : nullptr, step, c->pitch, 0.0, 0.0};
     return run<1>(c, "cheby_p", b, epi, fast);
@@ -968,7 +995,7 @@ int launch_cheby_calc_u(Chunk *c, int epi, bool fast) {
 
 template <int PC>
 static int ppcg_init(Chunk *c, int step, int epi) {
-    BodyPpcgInit<PC> b{c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->p, c->z, step, c->pitch};
+    BodyPpcgInit<PC> b{c->diag, c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->p, c->z, step, c->pitch};
     return run<1>(c, "ppcg_init", b, epi, false);
 }
 
@@ -983,15 +1010,15 @@ int launch_ppcg_init(Chunk *c, int step, int epi) {
 int launch_ppcg_init_sd(Chunk *c, double theta) {
     switch (c->cfg.precond) {
     case TL_PREC_JAC_BLOCK: {
-        BodyPpcgInitSd<TL_PREC_JAC_BLOCK> b{c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->sd, theta, c->pitch};
+        BodyPpcgInitSd<TL_PREC_JAC_BLOCK> b{c->diag, c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->sd, theta, c->pitch};
         return run<1>(c, "ppcg_init_sd", b, kEpiNone, false);
     }
     case TL_PREC_JAC_DIAG: {
-        BodyPpcgInitSd<TL_PREC_JAC_DIAG> b{c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->sd, theta, c->pitch};
+        BodyPpcgInitSd<TL_PREC_JAC_DIAG> b{c->diag, c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->sd, theta, c->pitch};
         return run<1>(c, "ppcg_init_sd", b, kEpiNone, false);
     }
     default: {
-        BodyPpcgInitSd<TL_PREC_NONE> b{c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->sd, theta, c->pitch};
+        BodyPpcgInitSd<TL_PREC_NONE> b{c->diag, c->r, c->mi, c->kx, c->ky, c->cp, c->bfp, c->sd, theta, c->pitch};
         return run<1>(c, "ppcg_init_sd", b, kEpiNone, false);
     }
     }
@@ -1008,13 +1035,13 @@ int launch_ppcg_init_sd_new(Chunk *c, double theta, bool fast) {
 }
 
 int launch_ppcg_update_r(Chunk *c, bool fast) {
-    BodyPpcgUpdateR b{c->sd, c->kx, c->ky, c->rtemp, c->pitch};
+    BodyPpcgUpdateR b{c->diag, c->sd, c->kx, c->ky, c->rtemp, c->pitch};
     return run<1>(c, "ppcg_update_r", b, kEpiNone, fast);
 }
 
 template <int PC>
 static int ppcg_sd(Chunk *c, int step, bool fast) {
-    BodyPpcgCalcSdNew<PC> b{c->rtemp, c->mi, c->kx, c->ky, c->cp, c->bfp, c->ch_alphas,
+    BodyPpcgCalcSdNew<PC> b{c->diag, c->rtemp, c->mi, c->kx, c->ky, c->cp, c->bfp, c->ch_alphas,
                             c->ch_betas, c->sd, c->utemp, step, c->pitch, 0.0, 0.0};
     return run<1>(c, "ppcg_sd", b, kEpiNone, fast);
 }

@@ -120,9 +120,11 @@ int capture(Chunk *c, int (*body)(Chunk *), int iters, cudaGraphExec_t *exec, lo
     return TL_OK;
 }
 
+}  // namespace
+
 // the profiling form of run_phase: the same iterations launched one kernel
 // at a time, each bracketed by CUDA events
-int run_phase_eager(Chunk *c, int (*body)(Chunk *), int iters, int *done_out) {
+static int run_phase_eager(Chunk *c, int (*body)(Chunk *), int iters, int *done_out) {
     int rc;
     for (;;) {
         for (int k = 0; k < iters; ++k)
@@ -162,8 +164,6 @@ int run_phase(Chunk *c, int (*body)(Chunk *), int iters, int phase, int *done_ou
     *done_out = c->sc_host->done;
     return TL_OK;
 }
-
-}  // namespace
 
 int solve_timestep(Chunk *c, tl_solve_info_t *info) {
     const auto t0 = std::chrono::steady_clock::now();

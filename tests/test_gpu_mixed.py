@@ -1,0 +1,61 @@
+"""The mixed-precision form (FP32 inner CG, FP64 iterative refinement) against
+the plain FP64 GPU solve and the CPU oracle.
+
+Bar: the same field_summary as plain FP64 CG within 1e-10 relative, and the
+same final FP64 residual test (||u0 - A u|| below tl_eps * ||r_0||, or the FP64
+floor).  The per-timestep error of u against the FP64 solution is checked and
+reported."""
+import numpy as np
+import pytest
+
+import tealeaf_cuda_gb300 as tl
+from tests import decks
+from tests.oracle_run import run_deck as oracle_run
+
+pytestmark = pytest.mark.gpu
+
+FS_RTOL = 1e-10
+
+
+def _solve_steps(deck, steps):
+    cfg = tl.parse_deck(deck)
+    out = []
+    with tl.Chunk(cfg) as ch:
+        ch.start()
+        for _ in range(steps):
+            info = ch.timestep()
+            out.append((info, ch.field_summary(), ch.interior("u").copy()))
+    return out
+
+
+@pytest.mark.parametrize("precond", ["none", "jac_diag"])
+@pytest.mark.parametrize("shape", [(64, 48), (200, 150)])
+def test_mixed_matches_fp64(precond, shape):
+    base = dict(x_cells=shape[0], y_cells=shape[1], end_step=3, tl_preconditioner_type=precond)
+    fp64 = _solve_steps(decks.make_deck(**base), 3)
+    mixed = _solve_steps(decks.make_deck(tl_precision="mixed", **base), 3)
+    for step, ((i64, s64, u64), (imx, smx, umx)) in enumerate(zip(fp64, mixed), start=1):
+        assert imx["status"] == 0
+        assert imx["outer_iters"] >= 1 and imx["inner_iters"] >= 1
+        for a, b in zip(s64, smx):
+            assert b == pytest.approx(a, rel=FS_RTOL), step
+        err = np.max(np.abs(umx - u64)) / np.max(np.abs(u64))
+        print(f"step {step}: outer {imx['outer_iters']} inner {imx['inner_iters']} "
+              f"(fp64 {i64['iterations']}) max|du|/max|u| = {err:.2e}")
+        assert err < 1e-9
+
+
+def test_mixed_matches_oracle_field_summary():
+    deck = decks.make_deck(x_cells=96, y_cells=96, end_step=4, tl_preconditioner_type="jac_diag")
+    steps, _ = oracle_run(deck)
+    recs, res = tl.run_deck(deck.replace("*endtea", "tl_precision mixed\n*endtea"))
+    assert res["status"] == 0
+    for k in ("vol", "mass", "ie", "temp"):
+        assert recs[-1][k] == pytest.approx(steps[-1][k], rel=FS_RTOL)
+
+
+def test_mixed_reaches_tl_eps_on_the_true_residual():
+    deck = decks.make_deck(x_cells=128, y_cells=128, end_step=1, tl_preconditioner_type="jac_diag",
+                           tl_eps=1e-12, tl_precision="mixed")
+    (info, _, _), = _solve_steps(deck, 1)
+    assert info["error_ratio"] < 1e-12
