@@ -111,6 +111,7 @@ typedef struct tl_config {
     int profiler_on, verbose, test_problem, cuda_device;
     int precision;                /* TL_PRECISION_* (tl_precision)           */
     double inner_eps;             /* mixed: inner FP32 relative tolerance    */
+    int warm_start;               /* 1: learned warm start (tl_warm_start)   */
     int nstates;
     tl_state_t states[TL_MAX_STATES];
 } tl_config_t;
@@ -131,6 +132,8 @@ typedef struct tl_solve_info {
     double eigmin, eigmax;
     double rx, ry;
     double seconds;               /* wall time of the solve on the host      */
+    int warm_used;                /* learned start kept (1) or fell back (0) */
+    double warm_ratio;            /* its residual / the plain start's        */
 } tl_solve_info_t;
 
 typedef struct tl_chunk tl_chunk_t;
@@ -200,6 +203,43 @@ int tl_default_chunk_init(const tl_config_t *cfg);
 int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long pitch,
                    double *result, void *stream);
 
+/* ------------------------------------------------ learned warm start
+ * No reference counterpart.  A residual network of six 3x3 convolutions
+ * (32 channels, GELU, BF16 tensor-core kernels) predicts u^{n+1} - u^n from
+ * (u^n, log density, Kx, Ky, dt); with cfg.warm_start set, tl_timestep starts
+ * from u^n + du when that lowers the residual and from u^n otherwise, and
+ * keeps the exit test tl_eps * (residual of the plain start).
+ *
+ * Parameters: FP32, flat, per layer W[9][coutp][cin] then b[coutp]; layers
+ * (cin, coutp) = (16,32) GELU, 4 x (32,32) x + GELU(conv x), (32,16) linear
+ * head (output channel 0).  A model file is the 8 bytes "TLWS0001", an
+ * int64 parameter count, then the FP32 parameters. */
+long long tl_warm_start_param_count(void);
+int tl_set_warm_start_model(tl_chunk_t *ch, const float *params, long long n);
+/* training data of the step just solved: FP32 [ny][nx][6] at device dst =
+ * (u^n/s, log density, log1p Kx, log1p Ky, 100 dt, (u^{n+1}-u^n)/s), s = max|u^n| */
+int tl_warm_start_features(tl_chunk_t *ch, float *dst);
+
+/* Network kernels on caller-owned device buffers (NHWC BF16 activations with
+ * a one-pixel zero halo, [B][H+2][W+2][C]; W a multiple of 16), used by the
+ * trainer.  mode 0: out = GELU(conv(in) + b), pre-activation to pre;
+ * 1: out = res + GELU(conv(in) + b); 2: outf[B][H][W] = conv(in)[0] + b[0];
+ * 3: out = res + conv(in) (data gradient, weights from tl_nn_pack's wb). */
+int tl_nn_conv(int mode, int cin, int coutp, const void *in, const void *w, const float *bias,
+               const void *res, void *out, void *pre, float *outf, int B, int H, int W, void *stream);
+int tl_nn_gelu_backward(const void *dh, const void *pre, void *dpre, int C, int B, int H, int W,
+                        void *stream);
+long long tl_nn_wgrad_partial_floats(int cin, int coutp, int B, int H, int W, int groups_per_cta);
+int tl_nn_wgrad(const void *dpre, const void *in, int cin, int coutp, float *partial, float *dw,
+                float *db, int B, int H, int W, int groups_per_cta, void *stream);
+int tl_nn_adam(float *p, const float *g, float *m, float *v, int n, float lr, float b1, float b2,
+               float eps, int step, void *stream);
+int tl_nn_pack(const float *w, void *wf, void *wb, int cin, int coutp, void *stream);
+int tl_nn_loss(const float *y, const float *t, void *dy, float *partial, int C, int B, int H, int W,
+               int margin, void *stream);
+int tl_nn_gather(const float *fields, const int *org, void *x, float *t, int F, int C, int Hs, int Ws,
+                 int B, int S, void *stream);
+
 /* ------------------------------------------------------- whole program
  * The main program of the reference (tea_leaf.f90 -> start.f90 ->
  * diffuse.f90) restated in C++: read a deck, set up the chunk, run the
@@ -222,6 +262,7 @@ typedef struct tl_run_options {
     int max_steps;                /* stop early after this many steps (0: no) */
     tl_step_record_t *records;    /* optional, one per step (step 0 first)   */
     int max_records;
+    const char *model_path;       /* warm start model file (tl_warm_start)   */
 } tl_run_options_t;
 
 typedef struct tl_run_result {

@@ -48,7 +48,7 @@ class Config(C.Structure):
                 ("ch_cg_presteps", C.c_int), ("ch_cg_epslim", C.c_double), ("ppcg_inner_steps", C.c_int),
                 ("profiler_on", C.c_int), ("verbose", C.c_int), ("test_problem", C.c_int),
                 ("cuda_device", C.c_int), ("precision", C.c_int), ("inner_eps", C.c_double),
-                ("nstates", C.c_int), ("states", State * MAX_STATES)]
+                ("warm_start", C.c_int), ("nstates", C.c_int), ("states", State * MAX_STATES)]
 
 
 class SolveInfo(C.Structure):
@@ -57,7 +57,8 @@ class SolveInfo(C.Structure):
                 ("inner_iters", C.c_int), ("initial_residual", C.c_double), ("error", C.c_double),
                 ("error_ratio", C.c_double), ("exact_error_ratio", C.c_double),
                 ("eigmin", C.c_double), ("eigmax", C.c_double), ("rx", C.c_double),
-                ("ry", C.c_double), ("seconds", C.c_double)]
+                ("ry", C.c_double), ("seconds", C.c_double), ("warm_used", C.c_int),
+                ("warm_ratio", C.c_double)]
 
 
 class StepRecord(C.Structure):
@@ -68,7 +69,8 @@ class StepRecord(C.Structure):
 
 class RunOptions(C.Structure):
     _fields_ = [("out_path", C.c_char_p), ("echo", C.c_int), ("legacy_abi", C.c_int),
-                ("max_steps", C.c_int), ("records", C.POINTER(StepRecord)), ("max_records", C.c_int)]
+                ("max_steps", C.c_int), ("records", C.POINTER(StepRecord)), ("max_records", C.c_int),
+                ("model_path", C.c_char_p)]
 
 
 class RunResult(C.Structure):
@@ -154,6 +156,19 @@ def load():
     lib.tl_default_chunk.restype = C.c_void_p
     lib.tl_default_chunk_init.argtypes = [C.POINTER(Config)]
     lib.tl_run_deck.argtypes = [C.c_char_p, C.POINTER(RunOptions), C.POINTER(RunResult)]
+    lib.tl_warm_start_param_count.restype = C.c_longlong
+    lib.tl_set_warm_start_model.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong]
+    lib.tl_warm_start_features.argtypes = [C.c_void_p, C.c_void_p]
+    _vp, _i, _f = C.c_void_p, C.c_int, C.c_float
+    lib.tl_nn_conv.argtypes = [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp]
+    lib.tl_nn_gelu_backward.argtypes = [_vp, _vp, _vp, _i, _i, _i, _i, _vp]
+    lib.tl_nn_wgrad_partial_floats.restype = C.c_longlong
+    lib.tl_nn_wgrad_partial_floats.argtypes = [_i, _i, _i, _i, _i, _i]
+    lib.tl_nn_wgrad.argtypes = [_vp, _vp, _i, _i, _vp, _vp, _vp, _i, _i, _i, _i, _vp]
+    lib.tl_nn_adam.argtypes = [_vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _i, _vp]
+    lib.tl_nn_pack.argtypes = [_vp, _vp, _vp, _i, _i, _vp]
+    lib.tl_nn_loss.argtypes = [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _vp]
+    lib.tl_nn_gather.argtypes = [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _i, _vp]
     for name, args in LEGACY_SIGNATURES.items():
         f = getattr(lib, name)
         f.argtypes = args
@@ -258,12 +273,14 @@ class Chunk:
         return load().tl_kernel_launches(self._h)
 
 
-def run_deck(text, legacy_abi=False, max_steps=0, out_path=None, echo=False, max_records=4096):
+def run_deck(text, legacy_abi=False, max_steps=0, out_path=None, echo=False, max_records=4096,
+             model_path=None):
     """Run a whole deck (tea_leaf.f90 main program); returns (records, result)."""
     lib = load()
     recs = (StepRecord * max_records)()
     opt = RunOptions(out_path.encode() if out_path else None, 1 if echo else 0,
-                     1 if legacy_abi else 0, max_steps, recs, max_records)
+                     1 if legacy_abi else 0, max_steps, recs, max_records,
+                     model_path.encode() if model_path else None)
     res = RunResult()
     rc = lib.tl_run_deck(text.encode(), C.byref(opt), C.byref(res))
     _check(rc, "tl_run_deck")

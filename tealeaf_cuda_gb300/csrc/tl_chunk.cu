@@ -68,6 +68,7 @@ static void chunk_release(Chunk *c) {
     if (!c) return;
     if (c->stream) cudaStreamSynchronize(c->stream);
     mixed_free(c);
+    warm_free(c);
     for (cudaGraphExec_t g : c->graphs)
         if (g) cudaGraphExecDestroy(g);
     for (void *p : c->allocations) cudaFree(p);
@@ -418,7 +419,18 @@ int tl_timestep(tl_chunk_t *ch, tl_solve_info_t *info) {
         set_error("tl_timestep: no chunk");
         return TL_ERR_STATE;
     }
-    if (ch->c->cfg.precision == TL_PRECISION_MIXED) return solve_timestep_mixed(ch->c, info);
+    const tl_config_t &cf = ch->c->cfg;
+    if (cf.precision == TL_PRECISION_MIXED) {
+        if (cf.solver == TL_SOLVER_PPCG) {
+            // FP64 flexible outer iteration, FP32 polynomial preconditioner
+            if (cf.reflective_boundary) {
+                set_error("tl_precision mixed does not support reflective_boundary");
+                return TL_ERR_ARG;
+            }
+            return solve_timestep(ch->c, info);
+        }
+        return solve_timestep_mixed(ch->c, info);
+    }
     return solve_timestep(ch->c, info);
 }
 
@@ -478,6 +490,22 @@ int tl_set_dt(tl_chunk_t *ch, double dt) {
 long long tl_kernel_launches(tl_chunk_t *ch) { return (ch && ch->c) ? ch->c->launches : 0; }
 
 void *tl_chunk_stream(tl_chunk_t *ch) { return (ch && ch->c) ? (void *)ch->c->stream : nullptr; }
+
+int tl_set_warm_start_model(tl_chunk_t *ch, const float *params, long long n) {
+    if (!ch || !ch->c || !params) {
+        set_error("tl_set_warm_start_model: bad argument");
+        return TL_ERR_ARG;
+    }
+    return warm_set_model(ch->c, params, n);
+}
+
+int tl_warm_start_features(tl_chunk_t *ch, float *dst) {
+    if (!ch || !ch->c || !dst) {
+        set_error("tl_warm_start_features: bad argument");
+        return TL_ERR_ARG;
+    }
+    return warm_features(ch->c, dst);
+}
 
 int tl_set_profiling(tl_chunk_t *ch, int on) {
     if (!ch || !ch->c) {

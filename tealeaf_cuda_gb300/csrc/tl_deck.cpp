@@ -225,6 +225,12 @@ void parse(const char *text, tl_config_t *c) {
                 else throw DeckError{TL_ERR_DECK, "Invalid tl_precision: " + v};
             }
             else if (w == "tl_inner_eps") c->inner_eps = d.rval();
+            else if (w == "tl_warm_start") {
+                std::string v = d.word(true);
+                if (v == "none" || v == "prev") c->warm_start = 0;
+                else if (v == "learned") c->warm_start = 1;
+                else throw DeckError{TL_ERR_DECK, "Invalid tl_warm_start: " + v};
+            }
             else if (w == "state") {
                 const int s = d.ival();
                 if (s < 1 || s > state_max) throw DeckError{TL_ERR_DECK, "Invalid state number"};

@@ -296,6 +296,32 @@ int legacy_start(const tl_config_t &cf, double *vol, double *mass, double *ie, d
     return (err && err[0]) ? TL_ERR_CUDA : TL_OK;
 }
 
+// warm start model file: "TLWS0001", int64 count, FP32 parameters
+int load_model(tl_chunk_t *ch, const char *path) {
+    if (!path) {
+        fprintf(stderr, "tea_leaf: tl_warm_start learned needs a model file\n");
+        return TL_ERR_ARG;
+    }
+    FILE *f = fopen(path, "rb");
+    if (!f) {
+        fprintf(stderr, "tea_leaf: cannot open model %s\n", path);
+        return TL_ERR_ARG;
+    }
+    char magic[8];
+    long long n = 0;
+    int rc = TL_ERR_ARG;
+    if (fread(magic, 1, 8, f) == 8 && memcmp(magic, "TLWS0001", 8) == 0 && fread(&n, 8, 1, f) == 1 &&
+        n == tl_warm_start_param_count()) {
+        std::vector<float> p((size_t)n);
+        if (fread(p.data(), sizeof(float), (size_t)n, f) == (size_t)n)
+            rc = tl_set_warm_start_model(ch, p.data(), n);
+    } else {
+        fprintf(stderr, "tea_leaf: %s is not a warm start model of this build\n", path);
+    }
+    fclose(f);
+    return rc;
+}
+
 }  // namespace
 
 extern "C" int tl_run_deck(const char *deck_text, const tl_run_options_t *opt, tl_run_result_t *res) {
@@ -329,6 +355,7 @@ extern "C" int tl_run_deck(const char *deck_text, const tl_run_options_t *opt, t
     } else {
         rc = tl_chunk_create(&cf, &ch);
         if (!rc) rc = tl_start(ch, &vol, &mass, &ie, &temp);
+        if (!rc && cf.warm_start) rc = load_model(ch, o.model_path);
     }
     if (rc) {
         fprintf(stderr, "tea_leaf: start failed: %s\n", tl_last_error());

@@ -124,6 +124,8 @@ struct Chunk {
     int grid_red;                // CTAs of the grid-stride kernels
     // mixed precision state (allocated on first use)
     void *mixed;
+    // learned warm start model and buffers (tl_warm.cu)
+    void *warm;
     double rx, ry;
     // per-kernel profiling (CUDA events around eager launches)
     bool profiling;
@@ -208,5 +210,17 @@ int run_phase(Chunk *c, int (*body)(Chunk *), int iters, int phase, int *done_ou
 constexpr int kPhaseMixedInner = 4;
 int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
+int mixed_ppcg_prepare(Chunk *c);  // FP32 operator + preconditioner copies
+int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
+// learned warm start (tl_warm.cu)
+void warm_free(Chunk *c);
+long long warm_param_count();
+int warm_set_model(Chunk *c, const float *params, long long n);
+bool warm_ready(Chunk *c);
+int warm_apply(Chunk *c);                 // u = u0 + du after common_init
+int warm_features(Chunk *c, float *dst);  // [ny][nx][6] features + target
+// learned start with fallback: after common_init, sets u and r, returns the
+// plain start's residual norm r0 in *r0 and the chosen start's r.r in *rr
+int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *rr);
 
 }  // namespace tl

@@ -32,8 +32,21 @@ namespace {
 
 struct Mixed {
     float *kx, *ky, *mi, *d, *r, *p, *w, *z;
+    float *sd[2], *rtemp, *utemp, *cp, *bfp;   // PPCG inner steps
+    double *partials;            // one per CTA of the vectorised kernels
+    unsigned int *counter;
+    int vtiles_x, vtiles;        // tiles of the vectorised kernels
     std::vector<void *> allocs;
 };
+
+// Vectorised FP32 kernels of the inner iteration: a lane owns four adjacent
+// columns (one float4, 16-byte aligned: the interior starts on a 128-byte
+// boundary) and walks kVRows rows keeping the rows above and below in
+// registers; x-neighbours across lanes come from warp shuffles.  A CTA is
+// 8 warps stacked in y: a 128-column x 64-row tile.
+constexpr int kVRows = 8;
+constexpr int kVCols = 128;
+constexpr int kVTileRows = kVRows * kBlockWarps;
 
 constexpr int kItersInner = 16;
 constexpr int kMaxOuter = 40;
@@ -151,30 +164,400 @@ __global__ void __launch_bounds__(kBlockThreads) k_mixed(Geo g, int pitch32, Bod
     }
 }
 
-// A x in FP32, difference form, on the m rows of a strip
-__device__ __forceinline__ void strip_apply32(const float *__restrict__ kx,
-                                              const float *__restrict__ ky,
-                                              const float *__restrict__ x, int pitch, int64_t base,
-                                              int m, float (&xc)[4], float (&ax)[4]) {
-    float xr[6], kyr[5];
+// ------------------------------------------------ vectorised inner kernels
+
+struct GeoV {
+    int nx, ny, h, pitch;
+    int tiles_x, tiles;
+};
+
+__device__ __forceinline__ float4 ld4(const float *__restrict__ f, int64_t i) {
+    return *reinterpret_cast<const float4 *>(f + i);
+}
+
+// store the first `nv` of four values (all four when nv == 4)
+__device__ __forceinline__ void st4(float *__restrict__ f, int64_t i, float4 v, int nv) {
+    if (nv >= 4) {
+        *reinterpret_cast<float4 *>(f + i) = v;
+    } else {
+        if (nv > 0) f[i] = v.x;
+        if (nv > 1) f[i + 1] = v.y;
+        if (nv > 2) f[i + 2] = v.z;
+    }
+}
+
+__device__ __forceinline__ float cell_apply(float c, float n, float s, float w, float e, float kyn,
+                                            float kyc, float kxe, float kxc) {
+    float v = fmaf(kyn, c - n, c);
+    v = fmaf(kyc, c - s, v);
+    v = fmaf(kxe, c - e, v);
+    return fmaf(kxc, c - w, v);
+}
+
+// block + grid reduction of a compensated sum; the last CTA runs the inner
+// epilogue.  Every thread of the CTA must call it.
+__device__ __forceinline__ void reduce_v(CSum acc, double *partials, unsigned int *counter,
+                                         DevScalars *sc, int epi) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = -1; k <= 4; ++k)
-        if (k <= m) xr[k + 1] = x[base + (int64_t)k * pitch];
+    for (int off = 16; off > 0; off >>= 1) {
+        CSum o;
+        o.s = __shfl_xor_sync(0xffffffffu, acc.s, off);
+        o.e = __shfl_xor_sync(0xffffffffu, acc.e, off);
+        acc = csum_merge(acc, o);
+    }
+    __shared__ double sh[kBlockWarps];
+    __shared__ int is_last;
+    if (lane == 0) sh[warp] = (double)acc.s + (double)acc.e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kBlockWarps; ++w) t += sh[w];
+        partials[blockIdx.x] = t;
+        __threadfence();
+        is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double t = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t += __ldcg(&partials[b]);
 #pragma unroll
-    for (int k = 0; k <= 4; ++k)
-        if (k <= m) kyr[k] = ky[base + (int64_t)k * pitch];
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    __syncthreads();
+    if (lane == 0) sh[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < kBlockWarps; ++w) tot += sh[w];
+        inner_epilogue(sc, epi, tot);
+        __threadfence();
+        *counter = 0u;
+    }
+}
+
+// w = A p on a 128 x 64 tile; sum p.w
+__global__ void __launch_bounds__(kBlockThreads) k_v_w(GeoV g, const float *__restrict__ p,
+                                                       const float *__restrict__ kx,
+                                                       const float *__restrict__ ky,
+                                                       float *__restrict__ w, double *partials,
+                                                       unsigned int *counter, DevScalars *sc) {
+    if (*(volatile const int *)&sc->done) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = (blockIdx.x % g.tiles_x) * kVCols + lane * 4;
+    const int j0 = (blockIdx.x / g.tiles_x) * kVTileRows + warp * kVRows;
+    const int nv = min(4, g.nx - c);           // valid columns of this lane
+    const bool live = c < g.nx + 4;            // lanes that load (the first one past nx reads the halo)
+    CSum acc = {0.f, 0.f};
+    if (j0 < g.ny) {
+        const int64_t P = g.pitch;
+        int64_t i = (int64_t)(c + g.h) + (int64_t)(j0 + g.h) * P;
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float4 xm = live ? ld4(p, i - P) : z4;
+        float4 x0 = live ? ld4(p, i) : z4;
+        float4 ky0 = live ? ld4(ky, i) : z4;
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (k < m) {
-            const int64_t i = base + (int64_t)k * pitch;
-            const float c = xr[k + 1];
-            float v = fmaf(kyr[k + 1], c - xr[k + 2], c);
-            v = fmaf(kyr[k], c - xr[k], v);
-            v = fmaf(kx[i + 1], c - x[i + 1], v);
-            v = fmaf(kx[i], c - x[i - 1], v);
-            ax[k] = v;
-            xc[k] = c;
+        for (int rr = 0; rr < kVRows; ++rr) {
+            if (j0 + rr >= g.ny) break;
+            const float4 xp = live ? ld4(p, i + P) : z4;
+            const float4 ky1 = live ? ld4(ky, i + P) : z4;
+            const float4 kxv = live ? ld4(kx, i) : z4;
+            float kxe = __shfl_down_sync(0xffffffffu, kxv.x, 1);
+            float xe = __shfl_down_sync(0xffffffffu, x0.x, 1);
+            float xw = __shfl_up_sync(0xffffffffu, x0.w, 1);
+            if (lane == 31 && live) {
+                kxe = kx[i + 4];
+                xe = p[i + 4];
+            }
+            if (lane == 0 && live) xw = p[i - 1];
+            float4 o;
+            o.x = cell_apply(x0.x, xp.x, xm.x, xw, x0.y, ky1.x, ky0.x, kxv.y, kxv.x);
+            o.y = cell_apply(x0.y, xp.y, xm.y, x0.x, x0.z, ky1.y, ky0.y, kxv.z, kxv.y);
+            o.z = cell_apply(x0.z, xp.z, xm.z, x0.y, x0.w, ky1.z, ky0.z, kxv.w, kxv.z);
+            o.w = cell_apply(x0.w, xp.w, xm.w, x0.z, xe, ky1.w, ky0.w, kxe, kxv.w);
+            if (nv > 0) {
+                st4(w, i, o, nv);
+                csum_add(acc, x0.x * o.x);
+                if (nv > 1) csum_add(acc, x0.y * o.y);
+                if (nv > 2) csum_add(acc, x0.z * o.z);
+                if (nv > 3) csum_add(acc, x0.w * o.w);
+            }
+            xm = x0;
+            x0 = xp;
+            ky0 = ky1;
+            i += P;
         }
+    }
+    reduce_v(acc, partials, counter, sc, kInW);
+}
+
+// d += alpha p; r -= alpha w; z = Mi r (DIAG) ; sum r.z
+template <bool DIAG>
+__global__ void __launch_bounds__(kBlockThreads) k_v_ur(GeoV g, float *__restrict__ d,
+                                                        float *__restrict__ r,
+                                                        float *__restrict__ z,
+                                                        const float *__restrict__ p,
+                                                        const float *__restrict__ w,
+                                                        const float *__restrict__ mi,
+                                                        double *partials, unsigned int *counter,
+                                                        DevScalars *sc) {
+    if (*(volatile const int *)&sc->done) return;
+    const float alpha = (float)sc->in_alpha;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = (blockIdx.x % g.tiles_x) * kVCols + lane * 4;
+    const int j0 = (blockIdx.x / g.tiles_x) * kVTileRows + warp * kVRows;
+    const int nv = min(4, g.nx - c);
+    CSum acc = {0.f, 0.f};
+    if (j0 < g.ny && nv > 0) {
+        const int64_t P = g.pitch;
+        int64_t i = (int64_t)(c + g.h) + (int64_t)(j0 + g.h) * P;
+#pragma unroll
+        for (int rr = 0; rr < kVRows; ++rr) {
+            if (j0 + rr >= g.ny) break;
+            const float4 pv = ld4(p, i), wv = ld4(w, i), rv0 = ld4(r, i), dv0 = ld4(d, i);
+            float4 dv, rv, zv;
+            dv.x = fmaf(alpha, pv.x, dv0.x);
+            dv.y = fmaf(alpha, pv.y, dv0.y);
+            dv.z = fmaf(alpha, pv.z, dv0.z);
+            dv.w = fmaf(alpha, pv.w, dv0.w);
+            rv.x = fmaf(-alpha, wv.x, rv0.x);
+            rv.y = fmaf(-alpha, wv.y, rv0.y);
+            rv.z = fmaf(-alpha, wv.z, rv0.z);
+            rv.w = fmaf(-alpha, wv.w, rv0.w);
+            if (DIAG) {
+                const float4 m = ld4(mi, i);
+                zv = make_float4(rv.x * m.x, rv.y * m.y, rv.z * m.z, rv.w * m.w);
+                st4(z, i, zv, nv);
+            } else {
+                zv = rv;
+            }
+            st4(d, i, dv, nv);
+            st4(r, i, rv, nv);
+            csum_add(acc, rv.x * zv.x);
+            if (nv > 1) csum_add(acc, rv.y * zv.y);
+            if (nv > 2) csum_add(acc, rv.z * zv.z);
+            if (nv > 3) csum_add(acc, rv.w * zv.w);
+            i += P;
+        }
+    }
+    reduce_v(acc, partials, counter, sc, kInUr);
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(kBlockThreads) k_v_p(GeoV g, float *__restrict__ p,
+                                                       const float *__restrict__ z,
+                                                       DevScalars *sc) {
+    if (*(volatile const int *)&sc->done) return;
+    const float beta = (float)sc->in_beta;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = (blockIdx.x % g.tiles_x) * kVCols + lane * 4;
+    const int j0 = (blockIdx.x / g.tiles_x) * kVTileRows + warp * kVRows;
+    const int nv = min(4, g.nx - c);
+    if (j0 >= g.ny || nv <= 0) return;
+    const int64_t P = g.pitch;
+    int64_t i = (int64_t)(c + g.h) + (int64_t)(j0 + g.h) * P;
+#pragma unroll
+    for (int rr = 0; rr < kVRows; ++rr) {
+        if (j0 + rr >= g.ny) break;
+        const float4 pv = ld4(p, i), zv = ld4(z, i);
+        float4 o;
+        o.x = fmaf(beta, pv.x, zv.x);
+        o.y = fmaf(beta, pv.y, zv.y);
+        o.z = fmaf(beta, pv.z, zv.z);
+        o.w = fmaf(beta, pv.w, zv.w);
+        st4(p, i, o, nv);
+        i += P;
+    }
+}
+
+// ------------------------------------ PPCG inner steps in FP32 (mixed form)
+//
+// The polynomial preconditioner of PPCG (tea_leaf_ppcg.f90:174-230):
+//   sd = z / theta, rtemp = r, utemp = sd;  for k = 1..inner:
+//   rtemp -= A sd; sd = alpha_k sd + beta_k M^-1 rtemp; utemp += sd;  z = utemp
+// runs here in FP32, one fused kernel per inner step (sd ping-pongs between
+// two buffers so the stencil reads the previous step); the last step writes
+// z back in FP64.  The outer flexible CG stays FP64, so the inexact FP32
+// preconditioner only changes how fast it converges, not what it converges
+// to.  Block-Jacobi strips (4 rows) are solved in registers, a float4 of
+// columns per lane; the FP32 copy keeps 1/diag of each strip's first row in
+// bfp (which the FP64 factorisation leaves unused there).
+
+// sd = (z or r) / theta; rtemp = r; utemp = sd
+template <bool USE_Z>
+__global__ void __launch_bounds__(kBlockThreads) k_pp_init(GeoV g, int pitch64, const double *__restrict__ r64,
+                                                           const double *__restrict__ z64, float *__restrict__ sd,
+                                                           float *__restrict__ rtemp, float *__restrict__ utemp,
+                                                           const DevScalars *__restrict__ sc) {
+    if (*(volatile const int *)&sc->done) return;
+    const double theta_r = 1.0 / sc->theta;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = (blockIdx.x % g.tiles_x) * kVCols + lane * 4;
+    const int j0 = (blockIdx.x / g.tiles_x) * kVTileRows + warp * kVRows;
+    const int nv = min(4, g.nx - c);
+    if (j0 >= g.ny || nv <= 0) return;
+#pragma unroll
+    for (int rr = 0; rr < kVRows; ++rr) {
+        const int j = j0 + rr;
+        if (j >= g.ny) break;
+        const int64_t i32 = (int64_t)(c + g.h) + (int64_t)(j + g.h) * g.pitch;
+        const int64_t i64 = (int64_t)(c + g.h) + (int64_t)(j + g.h) * pitch64;
+        float4 rv, sv;
+        float *rp = &rv.x, *sp = &sv.x;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double rq = q < nv ? r64[i64 + q] : 0.0;
+            const double zq = USE_Z ? (q < nv ? z64[i64 + q] : 0.0) : rq;
+            rp[q] = (float)rq;
+            sp[q] = (float)(zq * theta_r);
+        }
+        st4(rtemp, i32, rv, nv);
+        st4(sd, i32, sv, nv);
+        st4(utemp, i32, sv, nv);
+    }
+}
+
+// one inner step; PC: preconditioner, LAST: write z (FP64) = utemp instead
+// of rtemp / sd / utemp
+template <int PC, bool LAST>
+__global__ void __launch_bounds__(kBlockThreads) k_pp_step(
+    GeoV g, int pitch64, const float *__restrict__ sd_in, float *__restrict__ sd_out,
+    float *__restrict__ rtemp, float *__restrict__ utemp, const float *__restrict__ kx,
+    const float *__restrict__ ky, const float *__restrict__ mi, const float *__restrict__ cp,
+    const float *__restrict__ bfp, const double *__restrict__ alphas, const double *__restrict__ betas,
+    int step, double *__restrict__ z64, const DevScalars *__restrict__ sc) {
+    if (*(volatile const int *)&sc->done) return;
+    const float al = (float)alphas[step - 1], be = (float)betas[step - 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = (blockIdx.x % g.tiles_x) * kVCols + lane * 4;
+    const int j0 = (blockIdx.x / g.tiles_x) * kVTileRows + warp * kVRows;
+    const int nv = min(4, g.nx - c);
+    const bool live = c < g.nx + 4;
+    if (j0 >= g.ny) return;
+    const int64_t P = g.pitch;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    int64_t i = (int64_t)(c + g.h) + (int64_t)(j0 + g.h) * P;
+    float4 xm = live ? ld4(sd_in, i - P) : z4;
+    float4 x0 = live ? ld4(sd_in, i) : z4;
+    float4 ky0 = live ? ld4(ky, i) : z4;
+#pragma unroll
+    for (int s0 = 0; s0 < kVRows; s0 += 4) {
+        if (j0 + s0 >= g.ny) break;
+        const int m = min(4, g.ny - (j0 + s0));
+        float4 rt[4], sv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k >= m) break;
+            const int64_t ik = i + (int64_t)(s0 + k) * P;
+            const float4 xp = live ? ld4(sd_in, ik + P) : z4;
+            const float4 ky1 = live ? ld4(ky, ik + P) : z4;
+            const float4 kxv = live ? ld4(kx, ik) : z4;
+            float kxe = __shfl_down_sync(0xffffffffu, kxv.x, 1);
+            float xe = __shfl_down_sync(0xffffffffu, x0.x, 1);
+            float xw = __shfl_up_sync(0xffffffffu, x0.w, 1);
+            if (lane == 31 && live) {
+                kxe = kx[ik + 4];
+                xe = sd_in[ik + 4];
+            }
+            if (lane == 0 && live) xw = sd_in[ik - 1];
+            const float4 r0 = live ? ld4(rtemp, ik) : z4;
+            float4 o;
+            o.x = r0.x - cell_apply(x0.x, xp.x, xm.x, xw, x0.y, ky1.x, ky0.x, kxv.y, kxv.x);
+            o.y = r0.y - cell_apply(x0.y, xp.y, xm.y, x0.x, x0.z, ky1.y, ky0.y, kxv.z, kxv.y);
+            o.z = r0.z - cell_apply(x0.z, xp.z, xm.z, x0.y, x0.w, ky1.z, ky0.z, kxv.w, kxv.z);
+            o.w = r0.w - cell_apply(x0.w, xp.w, xm.w, x0.z, xe, ky1.w, ky0.w, kxe, kxv.w);
+            rt[k] = o;
+            sv[k] = x0;
+            xm = x0;
+            x0 = xp;
+            ky0 = ky1;
+        }
+        // z = M^-1 rtemp for the strip
+        float4 zz[4];
+        if (PC == TL_PREC_JAC_BLOCK) {
+            // forward sweep: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k
+            float4 dp[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k >= m) break;
+                const int64_t ik = i + (int64_t)(s0 + k) * P;
+                const float4 bf = live ? ld4(bfp, ik) : z4;
+                if (k == 0) {
+                    dp[0] = make_float4(rt[0].x * bf.x, rt[0].y * bf.y, rt[0].z * bf.z, rt[0].w * bf.w);
+                } else {
+                    const float4 kyk = live ? ld4(ky, ik) : z4;
+                    dp[k].x = fmaf(kyk.x, dp[k - 1].x, rt[k].x) * bf.x;
+                    dp[k].y = fmaf(kyk.y, dp[k - 1].y, rt[k].y) * bf.y;
+                    dp[k].z = fmaf(kyk.z, dp[k - 1].z, rt[k].z) * bf.z;
+                    dp[k].w = fmaf(kyk.w, dp[k - 1].w, rt[k].w) * bf.w;
+                }
+            }
+#pragma unroll
+            for (int k = 3; k >= 0; --k) {
+                if (k >= m) continue;
+                if (k == m - 1) {
+                    zz[k] = dp[k];
+                } else {
+                    const float4 cv = live ? ld4(cp, i + (int64_t)(s0 + k) * P) : z4;
+                    zz[k].x = fmaf(-cv.x, zz[k + 1].x, dp[k].x);
+                    zz[k].y = fmaf(-cv.y, zz[k + 1].y, dp[k].y);
+                    zz[k].z = fmaf(-cv.z, zz[k + 1].z, dp[k].z);
+                    zz[k].w = fmaf(-cv.w, zz[k + 1].w, dp[k].w);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k >= m) break;
+                if (PC == TL_PREC_JAC_DIAG) {
+                    const float4 mv = live ? ld4(mi, i + (int64_t)(s0 + k) * P) : z4;
+                    zz[k] = make_float4(rt[k].x * mv.x, rt[k].y * mv.y, rt[k].z * mv.z, rt[k].w * mv.w);
+                } else {
+                    zz[k] = rt[k];
+                }
+            }
+        }
+        // sd = alpha sd + beta z; utemp += sd
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k >= m) break;
+            const int64_t ik = i + (int64_t)(s0 + k) * P;
+            if (nv <= 0) continue;
+            float4 sn;
+            sn.x = fmaf(al, sv[k].x, be * zz[k].x);
+            sn.y = fmaf(al, sv[k].y, be * zz[k].y);
+            sn.z = fmaf(al, sv[k].z, be * zz[k].z);
+            sn.w = fmaf(al, sv[k].w, be * zz[k].w);
+            const float4 ut = ld4(utemp, ik);
+            const float4 un = make_float4(ut.x + sn.x, ut.y + sn.y, ut.z + sn.z, ut.w + sn.w);
+            if (LAST) {
+                const int64_t i64 = (int64_t)(c + g.h) + (int64_t)(j0 + s0 + k + g.h) * pitch64;
+                const float *uq = &un.x;
+                for (int q = 0; q < nv; ++q) z64[i64 + q] = (double)uq[q];
+            } else {
+                st4(rtemp, ik, rt[k], nv);
+                st4(sd_out, ik, sn, nv);
+                st4(utemp, ik, un, nv);
+            }
+        }
+    }
+}
+
+// FP32 copies of the preconditioner: Mi = 1/diag, block cp, and bfp with
+// 1/diag at each strip's first row
+__global__ void k_pp_convert(GeoV g, int pitch64, const double *__restrict__ dg, const double *__restrict__ cp64,
+                             const double *__restrict__ bfp64, float *__restrict__ mi, float *__restrict__ cp,
+                             float *__restrict__ bfp) {
+    const long long n = (long long)g.nx * g.ny;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(k % g.nx), j = (int)(k / g.nx);
+        const int64_t a = (int64_t)(i + g.h) + (int64_t)(j + g.h) * g.pitch;
+        const int64_t b = (int64_t)(i + g.h) + (int64_t)(j + g.h) * pitch64;
+        mi[a] = (float)(1.0 / dg[b]);
+        cp[a] = (float)cp64[b];
+        bfp[a] = (j % 4 == 0) ? (float)(1.0 / dg[b]) : (float)bfp64[b];
+    }
 }
 
 // Kx, Ky -> FP32; Mi = 1/diag(A) computed in FP64, stored in FP32
@@ -222,61 +605,6 @@ struct BodyInnerInit {  // r = (float) r64; z = M^-1 r; p = z; d = 0; sum r.z
     }
 };
 
-struct BodyInnerW {  // w = A p; sum p.w
-    const float *p, *kx, *ky;
-    float *w;
-    int pitch32;
-    __device__ void setup(DevScalars *) {}
-    __device__ void operator()(int64_t b32, int64_t, int m, CSum &acc) const {
-        float xc[4], ax[4];
-        strip_apply32(kx, ky, p, pitch32, b32, m, xc, ax);
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k < m) {
-                w[b32 + (int64_t)k * pitch32] = ax[k];
-                csum_add(acc, xc[k] * ax[k]);
-            }
-    }
-};
-
-template <bool DIAG>
-struct BodyInnerUr {  // d += alpha p; r -= alpha w; z = M^-1 r; sum r.z
-    float *d, *r, *z;
-    const float *p, *w, *mi;
-    int pitch32;
-    float alpha;
-    __device__ void setup(DevScalars *s) { alpha = (float)s->in_alpha; }
-    __device__ void operator()(int64_t b32, int64_t, int m, CSum &acc) const {
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k < m) {
-                const int64_t j = b32 + (int64_t)k * pitch32;
-                d[j] = fmaf(alpha, p[j], d[j]);
-                const float rv = fmaf(-alpha, w[j], r[j]);
-                r[j] = rv;
-                const float zv = DIAG ? rv * mi[j] : rv;
-                if (DIAG) z[j] = zv;
-                csum_add(acc, rv * zv);
-            }
-    }
-};
-
-struct BodyInnerP {  // p = z + beta p
-    float *p;
-    const float *z;
-    int pitch32;
-    float beta;
-    __device__ void setup(DevScalars *s) { beta = (float)s->in_beta; }
-    __device__ void operator()(int64_t b32, int64_t, int m, CSum &) const {
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k < m) {
-                const int64_t j = b32 + (int64_t)k * pitch32;
-                p[j] = fmaf(beta, p[j], z[j]);
-            }
-    }
-};
-
 struct BodyUpdateU {  // u += d (FP64)
     double *u;
     const float *d;
@@ -299,7 +627,8 @@ int mixed_alloc(Chunk *c) {
     Mixed *mx = new Mixed();
     c->mixed = mx;
     const size_t n = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows + 32;
-    float **arr[] = {&mx->kx, &mx->ky, &mx->mi, &mx->d, &mx->r, &mx->p, &mx->w, &mx->z};
+    float **arr[] = {&mx->kx, &mx->ky, &mx->mi,    &mx->d,     &mx->r,  &mx->p,  &mx->w,
+                     &mx->z,  &mx->sd[0], &mx->sd[1], &mx->rtemp, &mx->utemp, &mx->cp, &mx->bfp};
     for (float **a : arr) {
         void *p = nullptr;
         cudaError_t e = cudaMalloc(&p, n * sizeof(float));
@@ -308,6 +637,15 @@ int mixed_alloc(Chunk *c) {
         TL_CUDA(cudaMemsetAsync(p, 0, n * sizeof(float), c->stream));
         *a = (float *)p + c->lead;
     }
+    mx->vtiles_x = (c->nx + kVCols - 1) / kVCols;
+    mx->vtiles = mx->vtiles_x * ((c->ny + kVTileRows - 1) / kVTileRows);
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, sizeof(double) * (size_t)mx->vtiles + 256);
+    if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");
+    mx->allocs.push_back(p);
+    TL_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * (size_t)mx->vtiles + 256, c->stream));
+    mx->counter = (unsigned int *)p;
+    mx->partials = (double *)((char *)p + 256);
     return TL_OK;
 }
 
@@ -325,24 +663,108 @@ int run32(Chunk *c, const char *name, const Body &b, int epi, bool check_done) {
     return TL_OK;
 }
 
+// launch one vectorised kernel with the profiling bracket
+template <class F>
+int launch_v(Chunk *c, const char *name, F &&launch) {
+    int slot = -1;
+    if (c->profiling && !c->capturing) prof_begin(c, name, &slot);
+    launch();
+    if (slot >= 0) prof_end(c, slot);
+    c->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, name);
+    return TL_OK;
+}
+
 int inner_body(Chunk *c) {
     Mixed *mx = mixed_of(c);
     const bool diag = c->cfg.precond != TL_PREC_NONE;
+    const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
+    const unsigned grid = (unsigned)mx->vtiles;
+    cudaStream_t s = c->stream;
     int rc;
-    BodyInnerW bw{mx->p, mx->kx, mx->ky, mx->w, c->pitch};
-    if ((rc = run32(c, "mixed_w", bw, kInW, true))) return rc;
-    if (diag) {
-        BodyInnerUr<true> bu{mx->d, mx->r, mx->z, mx->p, mx->w, mx->mi, c->pitch, 0.f};
-        if ((rc = run32(c, "mixed_ur", bu, kInUr, true))) return rc;
-    } else {
-        BodyInnerUr<false> bu{mx->d, mx->r, mx->z, mx->p, mx->w, mx->mi, c->pitch, 0.f};
-        if ((rc = run32(c, "mixed_ur", bu, kInUr, true))) return rc;
-    }
-    BodyInnerP bp{mx->p, diag ? mx->z : mx->r, c->pitch, 0.f};
-    return run32(c, "mixed_p", bp, kInNone, true);
+    if ((rc = launch_v(c, "mixed_w", [&] {
+             k_v_w<<<grid, kBlockThreads, 0, s>>>(g, mx->p, mx->kx, mx->ky, mx->w, mx->partials,
+                                                   mx->counter, c->sc);
+         })))
+        return rc;
+    if ((rc = launch_v(c, "mixed_ur", [&] {
+             if (diag)
+                 k_v_ur<true><<<grid, kBlockThreads, 0, s>>>(g, mx->d, mx->r, mx->z, mx->p, mx->w,
+                                                             mx->mi, mx->partials, mx->counter, c->sc);
+             else
+                 k_v_ur<false><<<grid, kBlockThreads, 0, s>>>(g, mx->d, mx->r, mx->z, mx->p, mx->w,
+                                                              mx->mi, mx->partials, mx->counter, c->sc);
+         })))
+        return rc;
+    return launch_v(c, "mixed_p", [&] {
+        k_v_p<<<grid, kBlockThreads, 0, s>>>(g, mx->p, diag ? mx->z : mx->r, c->sc);
+    });
 }
 
 }  // namespace
+
+// FP32 copies of the operator and of the PPCG preconditioner, after cg_init
+// has built the FP64 ones
+int mixed_ppcg_prepare(Chunk *c) {
+    int rc;
+    if ((rc = mixed_alloc(c))) return rc;
+    Mixed *mx = mixed_of(c);
+    BodyConvert bc{c->kx, c->ky, mx->kx, mx->ky, mx->mi, c->pitch, c->pitch, c->nx, c->ny, c->h};
+    if ((rc = run32(c, "mixed_convert", bc, kInNone, false))) return rc;
+    const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
+    return launch_v(c, "mixed_pp_convert", [&] {
+        k_pp_convert<<<1216, 256, 0, c->stream>>>(g, c->pitch, c->diag, c->cp, c->bfp, mx->mi, mx->cp, mx->bfp);
+    });
+}
+
+// the inner steps of tea_leaf_ppcg.f90:174-230 in FP32; z (FP64) at the end
+int mixed_ppcg_inner(Chunk *c) {
+    Mixed *mx = mixed_of(c);
+    const int inner = c->cfg.ppcg_inner_steps;
+    if (!mx || inner < 1) {
+        set_error("mixed PPCG needs tl_ppcg_inner_steps >= 1 and a prepared chunk");
+        return TL_ERR_STATE;
+    }
+    const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
+    const unsigned grid = (unsigned)mx->vtiles;
+    cudaStream_t s = c->stream;
+    const int pc = c->cfg.precond;
+    int rc;
+    if ((rc = launch_v(c, "mixed_pp_init", [&] {
+             if (pc == TL_PREC_NONE)
+                 k_pp_init<false><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, c->r, c->z, mx->sd[0], mx->rtemp,
+                                                                 mx->utemp, c->sc);
+             else
+                 k_pp_init<true><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, c->r, c->z, mx->sd[0], mx->rtemp,
+                                                                mx->utemp, c->sc);
+         })))
+        return rc;
+    for (int st = 1; st <= inner; ++st) {
+        const float *si = mx->sd[(st - 1) & 1];
+        float *so = mx->sd[st & 1];
+        const bool last = st == inner;
+#define TL_PP_STEP(PC, L)                                                                              \
+    k_pp_step<PC, L><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, si, so, mx->rtemp, mx->utemp, mx->kx, \
+                                                    mx->ky, mx->mi, mx->cp, mx->bfp, c->ch_alphas,     \
+                                                    c->ch_betas, st, c->z, c->sc)
+        rc = launch_v(c, "mixed_pp_step", [&] {
+            if (pc == TL_PREC_JAC_BLOCK) {
+                if (last) TL_PP_STEP(TL_PREC_JAC_BLOCK, true);
+                else TL_PP_STEP(TL_PREC_JAC_BLOCK, false);
+            } else if (pc == TL_PREC_JAC_DIAG) {
+                if (last) TL_PP_STEP(TL_PREC_JAC_DIAG, true);
+                else TL_PP_STEP(TL_PREC_JAC_DIAG, false);
+            } else {
+                if (last) TL_PP_STEP(TL_PREC_NONE, true);
+                else TL_PP_STEP(TL_PREC_NONE, false);
+            }
+        });
+#undef TL_PP_STEP
+        if (rc) return rc;
+    }
+    return TL_OK;
+}
 
 void mixed_free(Chunk *c) {
     Mixed *mx = mixed_of(c);
@@ -378,12 +800,22 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
     DevScalars &h = *c->sc_host;
     memset(&h, 0, sizeof h);
     if ((rc = chunk_push_scalars(c))) return rc;
-    // r = u0 - A u, ||r||^2 (FP64)
-    if ((rc = launch_residual(c, kEpiResid))) return rc;
-    if ((rc = chunk_sync_scalars(c))) return rc;
-    const double r0 = h.initial_residual;
+    double r0, rn;
+    if (cf.warm_start) {
+        // learned start or the plain one, whichever has the smaller residual;
+        // the target stays tl_eps times the plain start's residual
+        double rr = 0.0;
+        if ((rc = warm_start_or_fallback(c, info, &r0, &rr))) return rc;
+        rn = sqrt(fabs(rr));
+    } else {
+        // r = u0 - A u, ||r||^2 (FP64)
+        if ((rc = launch_residual(c, kEpiResid))) return rc;
+        if ((rc = chunk_sync_scalars(c))) return rc;
+        r0 = h.initial_residual;
+        rn = r0;
+    }
     const double target = cf.eps * r0;
-    double rn = r0, rn_prev = 0.0;
+    double rn_prev = 0.0;
     int outer = 0, inner_total = 0;
     int status = TL_OK;
     while (true) {

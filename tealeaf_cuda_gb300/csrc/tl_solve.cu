@@ -45,6 +45,7 @@ int halo(Chunk *c, int field, int depth) {
 int ppcg_inner_steps(Chunk *c, bool fast) {
     const int inner = c->cfg.ppcg_inner_steps, hd = c->h;
     int rc;
+    if (c->cfg.precision == TL_PRECISION_MIXED) return mixed_ppcg_inner(c);
     if ((rc = halo(c, TL_FIELD_U, 1))) return rc;
     if (inner < 0) return TL_OK;
     if ((rc = launch_ppcg_init_sd_new(c, c->theta, fast))) return rc;
@@ -188,6 +189,12 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info) {
     if ((rc = halo(c, TL_FIELD_U, 1))) return rc;
 
     // scalars of this solve
+    // learned warm start: u = u^n + du if that lowers the residual, else the
+    // plain start; the exit test keeps the plain start's residual
+    double warm_r0 = 0.0, warm_rr = 0.0;
+    const bool warm = cf.warm_start != 0;
+    if (warm && (rc = warm_start_or_fallback(c, info, &warm_r0, &warm_rr))) return rc;
+
     DevScalars &h = *c->sc_host;
     memset(&h, 0, sizeof h);
     h.eps = cf.eps;
@@ -199,14 +206,20 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info) {
     h.ppcg_inner = cf.ppcg_inner_steps;
     h.n = 1;
     h.theta = c->theta;
+    if (warm) {
+        h.initial_residual = warm_r0;
+        h.old_error = warm_rr;
+    }
     if ((rc = chunk_push_scalars(c))) return rc;
 
-    if ((rc = launch_residual(c, kEpiResid))) return rc;
+    if (!warm && (rc = launch_residual(c, kEpiResid))) return rc;
     if (krylov) {
         if ((rc = launch_cg_init(c, kEpiRro))) return rc;
         int fl[7] = {0, 0, 0, 1, 1, 0, 0};
         if ((rc = chunk_update_halo(c, fl, 1))) return rc;
     }
+    // mixed-precision PPCG: FP32 copies of the operator and preconditioner
+    if (use_pp && cf.precision == TL_PRECISION_MIXED && (rc = mixed_ppcg_prepare(c))) return rc;
     if ((rc = chunk_sync_scalars(c))) return rc;
     info->initial_residual = h.initial_residual;
 

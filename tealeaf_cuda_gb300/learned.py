@@ -1,0 +1,324 @@
+"""Learned warm start: seeded random decks, trajectory data from the plain
+solver, the trainer of the residual network on the project's own BF16
+tensor-core kernels (tl_nn_* in csrc/tl_conv.cu), model files, and the
+evaluation of what the network saves over the plain start.
+
+Network (tl_warm.cu): inputs (u^n / s, log density, log1p Kx, log1p Ky,
+100 dt) with s = max|u^n|, six 3x3 convolutions of 32 channels (GELU, four
+residual blocks), output du / s; the solve starts from u^n + du when that
+lowers the residual and keeps tl_eps * (plain start residual) as its test.
+Torch only allocates device buffers here; every FLOP of the network runs in
+the library's kernels.
+"""
+import ctypes as C
+import math
+import struct
+
+import numpy as np
+
+from . import Chunk, load, parse_deck
+
+LAYERS = [(16, 32, 0)] + [(32, 32, 1)] * 4 + [(32, 16, 2)]  # (cin, coutp, conv mode)
+MASK64 = (1 << 64) - 1
+
+
+class SplitMix64:
+    """splitmix64 (Steele, Lea, Flood 2014), the counter-based generator of the decks."""
+
+    def __init__(self, seed):
+        self.state = seed & MASK64
+
+    def next(self):
+        self.state = (self.state + 0x9E3779B97F4A7C15) & MASK64
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+        return z ^ (z >> 31)
+
+    def uniform(self, a=0.0, b=1.0):
+        return a + (b - a) * (self.next() >> 11) / float(1 << 53)
+
+    def log_uniform(self, a, b):
+        return math.exp(self.uniform(math.log(a), math.log(b)))
+
+    def randint(self, n):
+        return self.next() % n
+
+
+def random_states(seed):
+    """3-8 axis-aligned rectangles of density U[0.05, 200] and energy
+    log-uniform [1e-4, 50] over a background drawn the same way."""
+    rng = SplitMix64(seed)
+    states = [{"index": 1, "density": rng.uniform(0.05, 200.0), "energy": rng.log_uniform(1e-4, 50.0)}]
+    for k in range(3 + rng.randint(6)):
+        x0, x1 = sorted((rng.uniform(0.0, 10.0), rng.uniform(0.0, 10.0)))
+        y0, y1 = sorted((rng.uniform(0.0, 10.0), rng.uniform(0.0, 10.0)))
+        x1, y1 = max(x1, x0 + 0.3), max(y1, y0 + 0.3)
+        states.append({"index": k + 2, "density": rng.uniform(0.05, 200.0),
+                       "energy": rng.log_uniform(1e-4, 50.0), "geometry": "rectangle",
+                       "xmin": x0, "xmax": x1, "ymin": y0, "ymax": y1})
+    return states
+
+
+def deck_text(states, n, steps, precond="jac_diag", eps=1e-15, extra=None):
+    lines = ["*tea"]
+    for st in states:
+        s = f"state {st['index']} density={st['density']!r} energy={st['energy']!r}"
+        if "geometry" in st:
+            s += (f" geometry={st['geometry']} xmin={st['xmin']!r} xmax={st['xmax']!r}"
+                  f" ymin={st['ymin']!r} ymax={st['ymax']!r}")
+        lines.append(s)
+    lines += [f"x_cells={n}", f"y_cells={n}", "xmin=0.0", "ymin=0.0", "xmax=10.0", "ymax=10.0",
+              "initial_timestep=0.004", f"end_step={steps}", "tl_max_iters=10000", "tl_use_cg",
+              f"tl_preconditioner_type {precond}", f"tl_eps {eps!r}", "summary_frequency 0"]
+    lines += list(extra or [])
+    lines.append("*endtea")
+    return "\n".join(lines) + "\n"
+
+
+def random_deck(seed, n, steps, **kw):
+    return deck_text(random_states(seed), n, steps, **kw)
+
+
+# ---------------------------------------------------------------- model
+
+def param_count():
+    return sum(9 * cin * co + co for cin, co, _ in LAYERS)
+
+
+def init_params(seed=0, head_scale=0.05):
+    rng = np.random.default_rng(seed)
+    out = []
+    for li, (cin, co, _) in enumerate(LAYERS):
+        cin_eff = 5 if li == 0 else cin
+        W = np.zeros((9, co, cin), dtype=np.float32)
+        std = math.sqrt(2.0 / (9 * cin_eff))
+        if li == len(LAYERS) - 1:
+            W[:, 0, :] = rng.normal(0.0, std * head_scale, (9, cin))
+        else:
+            W[:, :, :cin_eff] = rng.normal(0.0, std, (9, co, cin_eff))
+        out += [W.ravel(), np.zeros(co, dtype=np.float32)]
+    p = np.concatenate(out).astype(np.float32)
+    assert p.size == param_count()
+    return p
+
+
+def save_model(path, params):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    with open(path, "wb") as f:
+        f.write(b"TLWS0001")
+        f.write(struct.pack("<q", p.size))
+        f.write(p.tobytes())
+
+
+def load_model(path):
+    with open(path, "rb") as f:
+        assert f.read(8) == b"TLWS0001", "not a warm start model"
+        (n,) = struct.unpack("<q", f.read(8))
+        return np.frombuffer(f.read(4 * n), dtype=np.float32).copy()
+
+
+# ----------------------------------------------------------------- data
+
+def trajectories(seeds, n, steps, device="cuda:0", precond="jac_diag"):
+    """Solve `steps` timesteps of each seeded deck with the plain FP64 solver
+    and keep, per step, [n][n][6] = (features of u^n, (u^{n+1} - u^n) / s)."""
+    import torch
+    lib = load()
+    data = torch.empty((len(seeds) * steps, n, n, 6), dtype=torch.float32, device=device)
+    iters = []
+    k = 0
+    for seed in seeds:
+        cfg = parse_deck(random_deck(seed, n, steps, precond=precond))
+        with Chunk(cfg) as ch:
+            ch.start()
+            for _ in range(steps):
+                info = ch.timestep()
+                iters.append(info["iterations"])
+                rc = lib.tl_warm_start_features(ch._h, C.c_void_p(data[k].data_ptr()))
+                assert rc == 0
+                k += 1
+    torch.cuda.synchronize()
+    return data, iters
+
+
+# -------------------------------------------------------------- trainer
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class Trainer:
+    """Adam on FP32 master weights; forward and backward on tl_nn_* kernels
+    with BF16 activations and FP32 accumulation."""
+
+    def __init__(self, params, batch=16, crop=144, margin=8, lr=1e-3, device="cuda:0"):
+        import torch
+        self.torch = torch
+        self.lib = load()
+        self.B, self.S, self.margin, self.lr = batch, crop, margin, lr
+        self.dev = device
+        B, S = batch, crop
+        f32 = dict(dtype=torch.float32, device=device)
+        b16 = dict(dtype=torch.bfloat16, device=device)
+        self.params = torch.tensor(params, **f32)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.grad = torch.zeros_like(self.params)
+        self.views = []  # (W, b, dW, db, wf, wb) per layer
+        off = 0
+        for cin, co, _ in LAYERS:
+            nw = 9 * cin * co
+            self.views.append((self.params[off:off + nw], self.params[off + nw:off + nw + co],
+                               self.grad[off:off + nw], self.grad[off + nw:off + nw + co],
+                               torch.zeros(nw, **b16), torch.zeros(nw, **b16)))
+            off += nw + co
+        P = (B, S + 2, S + 2)
+        self.x = torch.zeros(P + (16,), **b16)
+        self.h = [torch.zeros(P + (32,), **b16) for _ in range(6)]
+        self.pre = [torch.zeros(P + (32,), **b16) for _ in range(5)]
+        self.y = torch.zeros((B, S, S), **f32)
+        self.t = torch.zeros((B, S, S), **f32)
+        self.dy = torch.zeros(P + (16,), **b16)
+        self.dh = [torch.zeros(P + (32,), **b16) for _ in range(2)]
+        self.dpre = torch.zeros(P + (32,), **b16)
+        self.gpc = 8
+        nmax = max(self.lib.tl_nn_wgrad_partial_floats(cin, co, B, S, S, self.gpc) for cin, co, _ in LAYERS)
+        self.partial = torch.zeros(int(nmax), **f32)
+        self.loss_part = torch.zeros(1216, **f32)
+        self.org = torch.zeros((B, 3), dtype=torch.int32, device=device)
+        self.step_no = 0
+        self.stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self.pack()
+
+    def check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what}: {self.lib.tl_last_error().decode()}")
+
+    def pack(self):
+        for (W, b, dW, db, wf, wb), (cin, co, _) in zip(self.views, LAYERS):
+            self.check(self.lib.tl_nn_pack(_p(W), _p(wf), _p(wb), cin, co, self.stream), "pack")
+
+    def forward(self):
+        L, B, S, s = self.lib, self.B, self.S, self.stream
+        hin = self.x
+        for li, (cin, co, mode) in enumerate(LAYERS):
+            W, b, dW, db, wf, wb = self.views[li]
+            if mode == 2:
+                self.check(L.tl_nn_conv(2, cin, co, _p(hin), _p(wf), _p(b), None, None, None, _p(self.y),
+                                        B, S, S, s), "head")
+            else:
+                out = self.h[li]
+                res = hin if mode == 1 else None
+                self.check(L.tl_nn_conv(mode, cin, co, _p(hin), _p(wf), _p(b), _p(res), _p(out),
+                                        _p(self.pre[li]), None, B, S, S, s), "conv")
+                hin = out
+        return self.y
+
+    def backward(self):
+        L, B, S, s = self.lib, self.B, self.S, self.stream
+        # head
+        W, b, dW, db, wf, wb = self.views[5]
+        self.check(L.tl_nn_wgrad(_p(self.dy), _p(self.h[4]), 32, 16, _p(self.partial), _p(dW), _p(db),
+                                 B, S, S, self.gpc, s), "wgrad head")
+        dh = self.dh[0]
+        self.check(L.tl_nn_conv(3, 16, 32, _p(self.dy), _p(wb), None, None, _p(dh), None, None, B, S, S, s),
+                   "dgrad head")
+        for li in range(4, 0, -1):
+            W, b, dW, db, wf, wb = self.views[li]
+            self.check(L.tl_nn_gelu_backward(_p(dh), _p(self.pre[li]), _p(self.dpre), 32, B, S, S, s), "gelu'")
+            self.check(L.tl_nn_wgrad(_p(self.dpre), _p(self.h[li - 1]), 32, 32, _p(self.partial), _p(dW),
+                                     _p(db), B, S, S, self.gpc, s), "wgrad")
+            dn = self.dh[1] if dh is self.dh[0] else self.dh[0]
+            self.check(L.tl_nn_conv(3, 32, 32, _p(self.dpre), _p(wb), None, _p(dh), _p(dn), None, None,
+                                    B, S, S, s), "dgrad")
+            dh = dn
+        W, b, dW, db, wf, wb = self.views[0]
+        self.check(L.tl_nn_gelu_backward(_p(dh), _p(self.pre[0]), _p(self.dpre), 32, B, S, S, s), "gelu'")
+        self.check(L.tl_nn_wgrad(_p(self.dpre), _p(self.x), 16, 32, _p(self.partial), _p(dW), _p(db),
+                                 B, S, S, self.gpc, s), "wgrad 1")
+
+    def loss(self):
+        """dy of the masked MSE; per-CTA partial sums of the squared error
+        land in loss_part (region_mse() reads them)"""
+        L = self.lib
+        self.check(L.tl_nn_loss(_p(self.y), _p(self.t), _p(self.dy), _p(self.loss_part), 16, self.B, self.S,
+                                self.S, self.margin, self.stream), "loss")
+
+    def step(self, data, rng):
+        """one Adam step on a batch of random crops of `data` ([N][H][W][6])"""
+        torch = self.torch
+        N, H, W, F = data.shape
+        S = self.S
+        org = np.stack([rng.integers(0, N, self.B), rng.integers(0, H - S + 1, self.B),
+                        rng.integers(0, W - S + 1, self.B)], axis=1).astype(np.int32)
+        self.org.copy_(torch.from_numpy(org))
+        self.check(self.lib.tl_nn_gather(_p(data), _p(self.org), _p(self.x), _p(self.t), F, 16, H, W, self.B,
+                                         S, self.stream), "gather")
+        self.forward()
+        self.loss()
+        self.backward()
+        self.step_no += 1
+        self.check(self.lib.tl_nn_adam(_p(self.params), _p(self.grad), _p(self.m), _p(self.v),
+                                       self.params.numel(), self.lr, 0.9, 0.999, 1e-8, self.step_no,
+                                       self.stream), "adam")
+        self.pack()
+
+    def region_mse(self):
+        cnt = self.B * (self.S - 2 * self.margin) ** 2
+        return float(self.loss_part.sum().item()) / cnt
+
+    def params_host(self):
+        return self.params.detach().cpu().numpy().copy()
+
+
+def train(data, iters=1500, batch=16, crop=144, lr=2e-3, seed=0, init=None, log_every=0):
+    """Train on trajectory data; returns (params, loss history)."""
+    params = init if init is not None else init_params(seed)
+    tr = Trainer(params, batch=batch, crop=crop, lr=lr, device=str(data.device))
+    rng = np.random.default_rng(seed)
+    hist = []
+    for it in range(iters):
+        tr.step(data, rng)
+        if log_every and (it % log_every == 0 or it == iters - 1):
+            hist.append((it, tr.region_mse()))
+    return tr.params_host(), hist
+
+
+# ------------------------------------------------------------ evaluation
+
+def solve_with(params, deck, steps):
+    """Per-step solve info of a deck, with the model (params) or the plain start (None)."""
+    lib = load()
+    cfg = parse_deck(deck)
+    cfg.warm_start = 1 if params is not None else 0
+    out = []
+    with Chunk(cfg) as ch:
+        ch.start()
+        if params is not None:
+            p = np.ascontiguousarray(params, dtype=np.float32)
+            assert lib.tl_set_warm_start_model(ch._h, C.c_void_p(p.ctypes.data), p.size) == 0
+        for _ in range(steps):
+            info = ch.timestep()
+            info["summary"] = ch.field_summary()
+            out.append(info)
+    return out
+
+
+def evaluate(params, seeds, n, steps, precond="jac_diag"):
+    """Compare the learned start with the plain one on held-out decks."""
+    rows = []
+    for seed in seeds:
+        deck = random_deck(seed, n, steps, precond=precond)
+        plain = solve_with(None, deck, steps)
+        warm = solve_with(params, deck, steps)
+        rows.append({"seed": seed,
+                     "plain_iters": [r["iterations"] for r in plain],
+                     "warm_iters": [r["iterations"] for r in warm],
+                     "warm_used": [r["warm_used"] for r in warm],
+                     "warm_ratio": [r["warm_ratio"] for r in warm],
+                     "plain_seconds": sum(r["seconds"] for r in plain),
+                     "warm_seconds": sum(r["seconds"] for r in warm),
+                     "summary_rel_diff": max(abs(a - b) / abs(a) for a, b in
+                                             zip(plain[-1]["summary"], warm[-1]["summary"]))})
+    return rows

@@ -23,7 +23,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["tl_kernels.cu", "tl_chunk.cu", "tl_solve.cu", "tl_legacy.cu", "tl_mixed.cu",
-              "tl_noalloc.cu"]
+              "tl_noalloc.cu", "tl_conv.cu", "tl_warm.cu"]
 CPP_SOURCES = ["tl_deck.cpp", "tl_driver.cpp", "tl_host_numerics.cpp"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE]

@@ -1,0 +1,80 @@
+"""The learned warm start on the GPU: the tensor-core forward pass and
+gradients of every layer against the CPU oracle of the network
+(oracle/nn_oracle.py, same bfloat16 rounding points, FP64 accumulation), a
+short training run on trajectories of seeded random decks, and what the
+trained network gains over the plain start on held-out decks."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import tealeaf_cuda_gb300 as tl
+from tealeaf_cuda_gb300 import learned
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import nn_oracle as nn  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def _trainer_with_batch(seed, B=2, S=32):
+    rng = np.random.default_rng(seed)
+    params = learned.init_params(seed, head_scale=1.0)
+    tr = learned.Trainer(params, batch=B, crop=S, margin=4)
+    x = np.zeros((B, S + 2, S + 2, 16), dtype=np.float32)
+    x[:, 1:-1, 1:-1, :5] = rng.normal(0, 1, (B, S, S, 5))
+    xb = torch.tensor(x).to(torch.bfloat16)
+    tr.x.copy_(xb.to(tr.x.device))
+    t = rng.normal(0, 0.3, (B, S, S)).astype(np.float32)
+    tr.t.copy_(torch.tensor(t).to(tr.t.device))
+    return tr, params, xb.float().numpy().astype(np.float64), t.astype(np.float64)
+
+
+def test_forward_matches_oracle():
+    tr, params, x, t = _trainer_with_batch(11)
+    y = tr.forward().detach().cpu().numpy()
+    yo, _ = nn.forward(params.astype(np.float64), x, quant=True)
+    assert _rel(y, yo) < 1e-2
+
+
+def test_gradients_match_oracle():
+    tr, params, x, t = _trainer_with_batch(12)
+    tr.forward()
+    tr.loss()
+    tr.backward()
+    torch.cuda.synchronize()
+    g = tr.grad.detach().cpu().numpy()
+    yo, cache = nn.forward(params.astype(np.float64), x, quant=True)
+    _, dy = nn.loss_and_dy(yo, t, 4, quant=True)
+    grads = nn.backward(params.astype(np.float64), cache, dy, quant=True)
+    off = 0
+    for li, ((cin, co, _), (dw, db)) in enumerate(zip(nn.LAYERS, grads)):
+        nw = 9 * co * cin
+        gw, gb = g[off:off + nw].reshape(9, co, cin), g[off + nw:off + nw + co]
+        assert _rel(gw, dw) < 3e-2, (li, _rel(gw, dw))
+        assert _rel(gb, db) < 3e-2, (li, _rel(gb, db))
+        off += nw + co
+
+
+def test_training_and_warm_start_gain():
+    n, steps = 256, 4
+    data, iters = learned.trajectories(range(100, 112), n, steps)
+    params, hist = learned.train(data, iters=300, batch=16, crop=144, lr=2e-3, seed=0, log_every=50)
+    assert hist[-1][1] < 0.5 * hist[0][1], hist
+    rows = learned.evaluate(params, [5000, 5001], n, 3)
+    plain = sum(sum(r["plain_iters"]) for r in rows)
+    warm = sum(sum(r["warm_iters"]) for r in rows)
+    used = sum(sum(r["warm_used"]) for r in rows)
+    print(f"loss {hist[0][1]:.3e} -> {hist[-1][1]:.3e}; CG iterations plain {plain} learned {warm}; "
+          f"learned start kept in {used} of {sum(len(r['warm_used']) for r in rows)} solves; "
+          f"residual ratios {[r['warm_ratio'] for r in rows]}")
+    assert warm < plain
+    for r in rows:
+        assert r["summary_rel_diff"] < 1e-10

@@ -59,3 +59,21 @@ def test_mixed_reaches_tl_eps_on_the_true_residual():
                            tl_eps=1e-12, tl_precision="mixed")
     (info, _, _), = _solve_steps(deck, 1)
     assert info["error_ratio"] < 1e-12
+
+
+@pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
+def test_mixed_ppcg_matches_fp64(precond):
+    """PPCG with its polynomial preconditioner (the 10 inner steps) in FP32:
+    the outer flexible CG stays FP64 and reaches the same answer."""
+    base = dict(x_cells=96, y_cells=80, end_step=3, tl_preconditioner_type=precond, tl_use_cg=False,
+                tl_use_ppcg=True, tl_ppcg_inner_steps=10, tl_ch_cg_presteps=10, tl_ch_cg_epslim=1.0e10)
+    fp64 = _solve_steps(decks.make_deck(**base), 3)
+    mixed = _solve_steps(decks.make_deck(tl_precision="mixed", **base), 3)
+    for step, ((i64, s64, u64), (imx, smx, umx)) in enumerate(zip(fp64, mixed), start=1):
+        assert imx["status"] == 0
+        for a, b in zip(s64, smx):
+            assert b == pytest.approx(a, rel=FS_RTOL), step
+        err = np.max(np.abs(umx - u64)) / np.max(np.abs(u64))
+        print(f"ppcg {precond} step {step}: outer its fp64 {i64['iterations']} mixed {imx['iterations']}, "
+              f"max|du|/max|u| = {err:.2e}")
+        assert err < 1e-9
