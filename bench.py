@@ -81,7 +81,7 @@ def make_deck(n, solver="cg", precond="jac_diag", max_iters=10000, end_step=1000
             f"x_cells={n}\ny_cells={n}\nxmin=0.0\nymin=0.0\nxmax=10.0\nymax=10.0\n"
             f"initial_timestep=0.004\nend_step={end_step}\ntl_max_iters={max_iters}\n"
             f"tl_use_{solver}\ntl_preconditioner_type {precond}\ntl_eps 1.0e-15\n"
-            f"tl_precision {precision}\nsummary_frequency 0\n*endtea\n")
+            f"tl_ppcg_inner_steps 10\ntl_precision {precision}\nsummary_frequency 0\n*endtea\n")
 
 
 # ------------------------------------------------------------------ clocks

@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <math.h>
 #include <time.h>
 
 static char *slurp(const char *path) {
@@ -32,14 +33,25 @@ static double now(void) {
     return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
 }
 
+/* a double as a JSON number; NaN and infinities in the spelling Python's
+ * json module reads */
+static void num(const char *key, double v) {
+    if (isnan(v)) printf(", \"%s\": NaN", key);
+    else if (isinf(v)) printf(", \"%s\": %sInfinity", key, v < 0 ? "-" : "");
+    else printf(", \"%s\": %.17g", key, v);
+}
+
 static void print_step(const ora_step_result *r, double wall) {
     printf("{\"kind\": \"step\", \"step\": %d, \"iterations\": %d, \"ppcg_inner\": %d, "
-           "\"error_ratio\": %.17g, \"switch_n\": %d, \"est_itc\": %d, \"wall\": %.6f",
-           r->step, r->iterations, r->ppcg_inner_iters, r->error_ratio, r->switch_n,
-           r->est_itc, wall);
-    if (r->has_summary)
-        printf(", \"vol\": %.17g, \"mass\": %.17g, \"ie\": %.17g, \"temp\": %.17g", r->vol,
-               r->mass, r->ie, r->temp);
+           "\"switch_n\": %d, \"est_itc\": %d, \"wall\": %.6f",
+           r->step, r->iterations, r->ppcg_inner_iters, r->switch_n, r->est_itc, wall);
+    num("error_ratio", r->error_ratio);
+    if (r->has_summary) {
+        num("vol", r->vol);
+        num("mass", r->mass);
+        num("ie", r->ie);
+        num("temp", r->temp);
+    }
     printf("}\n");
     fflush(stdout);
 }

@@ -61,13 +61,17 @@ def random_states(seed):
 
 
 def deck_text(states, n, steps, precond="jac_diag", eps=1e-15, extra=None):
+    """A tea.in deck.  The reader keeps only the first 100 characters of a
+    line (parse.f90:132, FMT='(a100)'), so each state is split over lines
+    joined by the parser's `\\` continuation."""
     lines = ["*tea"]
     for st in states:
-        s = f"state {st['index']} density={st['density']!r} energy={st['energy']!r}"
+        lines.append(f"state {st['index']} density={st['density']!r} energy={st['energy']!r}" +
+                     (" \\" if "geometry" in st else ""))
         if "geometry" in st:
-            s += (f" geometry={st['geometry']} xmin={st['xmin']!r} xmax={st['xmax']!r}"
-                  f" ymin={st['ymin']!r} ymax={st['ymax']!r}")
-        lines.append(s)
+            lines.append(f"  geometry={st['geometry']} xmin={st['xmin']!r} xmax={st['xmax']!r} \\")
+            lines.append(f"  ymin={st['ymin']!r} ymax={st['ymax']!r}")
+    assert all(len(l) <= 100 for l in lines)
     lines += [f"x_cells={n}", f"y_cells={n}", "xmin=0.0", "ymin=0.0", "xmax=10.0", "ymax=10.0",
               "initial_timestep=0.004", f"end_step={steps}", "tl_max_iters=10000", "tl_use_cg",
               f"tl_preconditioner_type {precond}", f"tl_eps {eps!r}", "summary_frequency 0"]
@@ -138,6 +142,39 @@ def trajectories(seeds, n, steps, device="cuda:0", precond="jac_diag"):
                 rc = lib.tl_warm_start_features(ch._h, C.c_void_p(data[k].data_ptr()))
                 assert rc == 0
                 k += 1
+    torch.cuda.synchronize()
+    return data, iters
+
+
+def trajectory_crops(seeds, n, steps, crops_per_step, crop=144, seed=0, device="cuda:0",
+                     precond="jac_diag", every=1):
+    """Like trajectories(), but keeps `crops_per_step` random crop x crop
+    windows of every `every`-th step instead of whole fields (a 3x3-conv
+    network is translation-equivariant, so crops are enough to train it and
+    keep large grids in memory).  Returns ([N][crop][crop][6], iterations)."""
+    import torch
+    lib = load()
+    rng = np.random.default_rng(seed)
+    kept = sum(1 for s in range(steps) if s % every == 0)
+    data = torch.empty((len(seeds) * kept * crops_per_step, crop, crop, 6), dtype=torch.float32,
+                       device=device)
+    full = torch.empty((n, n, 6), dtype=torch.float32, device=device)
+    iters = []
+    k = 0
+    for sd in seeds:
+        cfg = parse_deck(random_deck(sd, n, steps, precond=precond))
+        with Chunk(cfg) as ch:
+            ch.start()
+            for s in range(steps):
+                info = ch.timestep()
+                iters.append(info["iterations"])
+                if s % every:
+                    continue
+                assert lib.tl_warm_start_features(ch._h, C.c_void_p(full.data_ptr())) == 0
+                for _ in range(crops_per_step):
+                    y0, x0 = rng.integers(0, n - crop + 1, 2)
+                    data[k].copy_(full[y0:y0 + crop, x0:x0 + crop])
+                    k += 1
     torch.cuda.synchronize()
     return data, iters
 
@@ -322,3 +359,67 @@ def evaluate(params, seeds, n, steps, precond="jac_diag"):
                      "summary_rel_diff": max(abs(a - b) / abs(a) for a, b in
                                              zip(plain[-1]["summary"], warm[-1]["summary"]))})
     return rows
+
+
+def main(argv=None):
+    """python -m tealeaf_cuda_gb300.learned train|evaluate ...
+
+    train:    trajectories of seeded random decks -> model file (+ JSON report)
+    evaluate: plain vs learned start on held-out seeds (JSON report)"""
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser(prog="python -m tealeaf_cuda_gb300.learned")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    t = sub.add_parser("train")
+    t.add_argument("--decks", type=int, default=200)
+    t.add_argument("--first-seed", type=int, default=0)
+    t.add_argument("--steps", type=int, default=30)
+    t.add_argument("--every", type=int, default=1)
+    t.add_argument("--n", type=int, default=2048)
+    t.add_argument("--crops", type=int, default=4)
+    t.add_argument("--iters", type=int, default=3000)
+    t.add_argument("--batch", type=int, default=32)
+    t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--out", required=True)
+    t.add_argument("--report", default=None)
+    e = sub.add_parser("evaluate")
+    e.add_argument("--model", required=True)
+    e.add_argument("--seeds", default="10000-10049")
+    e.add_argument("--n", type=int, default=2048)
+    e.add_argument("--steps", type=int, default=3)
+    e.add_argument("--report", default=None)
+    a = ap.parse_args(argv)
+    if a.cmd == "train":
+        t0 = time.time()
+        seeds = list(range(a.first_seed, a.first_seed + a.decks))
+        data, iters = trajectory_crops(seeds, a.n, a.steps, a.crops, every=a.every)
+        t1 = time.time()
+        params, hist = train(data, iters=a.iters, batch=a.batch, lr=a.lr, log_every=max(1, a.iters // 20))
+        t2 = time.time()
+        save_model(a.out, params)
+        rep = {"decks": a.decks, "steps": a.steps, "n": a.n, "samples": int(data.shape[0]),
+               "plain_iterations_mean": float(np.mean(iters)), "data_seconds": t1 - t0,
+               "train_seconds": t2 - t1, "loss": hist}
+        print(json.dumps(rep))
+        if a.report:
+            json.dump(rep, open(a.report, "w"), indent=1)
+    else:
+        lo, hi = (int(x) for x in a.seeds.split("-"))
+        rows = evaluate(load_model(a.model), list(range(lo, hi + 1)), a.n, a.steps)
+        plain = sum(sum(r["plain_iters"]) for r in rows)
+        warm = sum(sum(r["warm_iters"]) for r in rows)
+        rep = {"n": a.n, "steps": a.steps, "seeds": a.seeds, "plain_iterations": plain,
+               "learned_iterations": warm, "iteration_ratio": warm / max(plain, 1),
+               "plain_seconds": sum(r["plain_seconds"] for r in rows),
+               "learned_seconds": sum(r["warm_seconds"] for r in rows),
+               "learned_start_kept": sum(sum(r["warm_used"]) for r in rows),
+               "solves": sum(len(r["warm_used"]) for r in rows),
+               "max_summary_rel_diff": max(r["summary_rel_diff"] for r in rows), "decks": rows}
+        print(json.dumps({k: v for k, v in rep.items() if k != "decks"}))
+        if a.report:
+            json.dump(rep, open(a.report, "w"), indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -64,11 +64,11 @@ def test_gradients_match_oracle():
 
 
 def test_training_and_warm_start_gain():
-    n, steps = 256, 4
-    data, iters = learned.trajectories(range(100, 112), n, steps)
-    params, hist = learned.train(data, iters=300, batch=16, crop=144, lr=2e-3, seed=0, log_every=50)
+    n, steps = 512, 6
+    data, iters = learned.trajectory_crops(range(100, 124), n, steps, crops_per_step=4)
+    params, hist = learned.train(data, iters=400, batch=16, crop=144, lr=2e-3, seed=0, log_every=50)
     assert hist[-1][1] < 0.5 * hist[0][1], hist
-    rows = learned.evaluate(params, [5000, 5001], n, 3)
+    rows = learned.evaluate(params, [5000, 5001, 5002], n, 3)
     plain = sum(sum(r["plain_iters"]) for r in rows)
     warm = sum(sum(r["warm_iters"]) for r in rows)
     used = sum(sum(r["warm_used"]) for r in rows)
