@@ -1,32 +1,43 @@
 #!/usr/bin/env python
 """Benchmark of the TeaLeaf implicit solve on GB300.
 
-Workload: the standard five-state deck (10 x 10 domain, dt 0.004) at
-4096 x 4096 cells, FP64 CG with the diagonal Jacobi preconditioner, solved to
-tl_eps 1e-15 with tl_max_iters 10000.  A step is one timestep: one complete
-implicit solve (tea_leaf(), tea_solve.f90:37) plus the field summary, with
-every field resident in HBM.  The metric is cell-iterations per second:
-cells x solver iterations / time, summed over the K timed steps; the time to
-solution per step is reported beside it.
+Workload (default): the standard five-state deck (10 x 10 domain,
+dt 0.004) at 8192 x 8192 cells solved to tl_eps 1e-15, timesteps 1..K of a
+fresh run, by two methods on the same GPU:
+  headline  PPCG with the 4-row block-Jacobi preconditioner and 10 inner
+            Chebyshev steps, FP32 inner steps inside the FP64 outer solve,
+            started by the learned warm start (network + previous step,
+            Galerkin-combined);
+  plain     FP64 CG with the diagonal Jacobi preconditioner from u = u^n
+            (the reference's method; its iteration counts define the work).
+A step is one timestep: one complete implicit solve (tea_leaf(),
+tea_solve.f90:37), with every field resident in HBM.  The metric is
+plain-CG cell-iterations per second: cells x (iterations the plain FP64 CG
+takes for those timesteps) / time, so a method that reaches tl_eps in less
+time scores higher in proportion; the time to solution per step of both
+methods and the field_summary difference between them are reported beside
+it.  --solver/--precond/--precision/--warm select another headline method.
 
-Legs (all in one run, one JSON line):
-  value      K device-resident solves (CUDA graphs), timed with CUDA events on
-             the library's stream, fields resident in HBM.  Every field of the
-             4096^2 problem is larger than L2 (134 MB each), so no flush is
-             needed between steps.
-  roofline   K more solves with per-kernel CUDA events (eager launches); the
-             dominant kernel's algorithmic bytes per launch / its mean launch
-             time, against the measured HBM copy bandwidth.
-  e2e        K more solves through the C-ABI with host buffers: density and
-             energy copied host->device before and energy copied back after
-             every solve, inside the timed region.
-  cpu_baseline  the CPU oracle (oracle/) on the host cores, one timestep of
-             the same deck capped at a fixed iteration count.
+Legs (one JSON line):
+  value      K device-resident solves of the headline method (CUDA graphs),
+             timed with CUDA events on the library's stream.  Every field is
+             larger than L2 (537 MB each at 8192^2), so no flush is needed
+             between steps.
+  plain      K solves of FP64 CG + jac_diag from a fresh start (timed the
+             same way; gives the work count and the baseline time).
+  roofline   K more headline solves with per-kernel CUDA events (eager
+             launches); the dominant kernel's algorithmic bytes per launch /
+             its mean launch time, against the measured HBM copy bandwidth.
+  e2e        K more headline solves through the C-ABI with host buffers:
+             density and energy copied host->device before and energy copied
+             back after every solve, inside the timed region.
+  cpu_baseline  the CPU oracle (oracle/) on the host cores: one timestep of
+             the same deck by CG + jac_diag, capped at --cpu-iters iterations.
 
 --impl reference runs the reference algorithm on the host CPU instead (the
 reference has no CPU implementation of this path, so the oracle's
-restatement of it is timed, all host threads), on the same deck, each step a
-timestep capped at --ref-iters iterations.
+restatement of it is timed, all host threads): FP64 CG + jac_diag on the same
+deck, each step a timestep capped at --ref-iters iterations.
 
 Multi-GPU: one process per GPU (torchrun); each rank solves its own replica
 (the single-chunk solve has no data-parallel split), value = all ranks'
@@ -46,6 +57,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "time-to-solution & cell-iters/s at tl_eps: mixed+learned vs plain FP64 CG, 1 GB300"
+DEFAULT_MODEL = os.path.join(ROOT, "tealeaf_cuda_gb300", "warm_start.tlws")
 
 STATES = """state 1 density=100.0 energy=0.0001
 state 2 density=0.1 energy=25.0 geometry=rectangle xmin=0.0 xmax=1.0 ymin=1.0 ymax=2.0
@@ -54,8 +66,9 @@ state 4 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=6.0 ymin=1.0 yma
 state 5 density=0.1 energy=0.1 geometry=rectangle xmin=5.0 xmax=10.0 ymin=7.0 ymax=8.0
 """
 
-# algorithmic bytes per interior cell of each FP64 kernel: every array the
-# kernel must read or write, counted once (halos ignored)
+# algorithmic bytes per interior cell of each kernel: every array the kernel
+# must read or write, counted once (halos ignored); FP64 arrays 8 bytes, FP32
+# arrays 4
 BYTES_PER_CELL = {
     "cg_w": 32,          # read p, Kx, Ky; write w
     "cg_ur": 64,         # jac_diag: read u, p, r, w, Mi; write u, r, z
@@ -66,6 +79,8 @@ BYTES_PER_CELL = {
     "diag": 24,          # read Kx, Ky; write diag
     "field_summary": 32,
     "finalise": 24,
+    "ppcg_p": 24,        # read z, p; write p
+    "copy": 16,          # read src; write dst
     # mixed precision: FP32 inner iteration (4-byte elements)
     "mixed_w": 16,       # read p, Kx, Ky; write w
     "mixed_ur": 32,      # jac_diag: read d, p, r, w, Mi; write d, r, z
@@ -73,15 +88,28 @@ BYTES_PER_CELL = {
     "mixed_init": 28,    # read r (FP64), Mi; write r, z, p, d
     "mixed_update_u": 20,  # read u (FP64), d; write u (FP64)
     "mixed_convert": 40,   # read Kx, Ky (FP64); write Kx, Ky, Mi (FP32)
+    "mixed_pp_init": 28,   # read r, z (FP64); write sd, rtemp, utemp
 }
 
 
-def make_deck(n, solver="cg", precond="jac_diag", max_iters=10000, end_step=100000, precision="fp64"):
+def bytes_per_cell(kernel, precond):
+    """algorithmic bytes per cell of `kernel` under preconditioner `precond`"""
+    if kernel == "mixed_pp_step":
+        # read sd, Kx, Ky, rtemp, utemp + the preconditioner (Mi; or cp and
+        # 1/b of the strip solve); write sd', rtemp, utemp (an inner step
+        # before the last)
+        return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
+    return BYTES_PER_CELL.get(kernel)
+
+
+def make_deck(n, solver="cg", precond="jac_diag", max_iters=10000, end_step=100000, precision="fp64",
+              warm="none"):
     return ("*tea\n" + STATES +
             f"x_cells={n}\ny_cells={n}\nxmin=0.0\nymin=0.0\nxmax=10.0\nymax=10.0\n"
             f"initial_timestep=0.004\nend_step={end_step}\ntl_max_iters={max_iters}\n"
             f"tl_use_{solver}\ntl_preconditioner_type {precond}\ntl_eps 1.0e-15\n"
-            f"tl_ppcg_inner_steps 10\ntl_precision {precision}\nsummary_frequency 0\n*endtea\n")
+            f"tl_ppcg_inner_steps 10\ntl_precision {precision}\ntl_warm_start {warm}\n"
+            f"summary_frequency 0\n*endtea\n")
 
 
 # ------------------------------------------------------------------ clocks
@@ -212,26 +240,55 @@ def run_reference(args):
     secs = sum(w for _, w in timed)
     value = n * n * its / secs
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-iters/s",
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "plain-CG cell-iters/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * secs / len(timed), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (standard five-state deck)",
-        "config": {"workload": f"standard deck {n}x{n}, CG + jac_diag, FP64, tl_eps 1e-15, "
-                               f"each step one timestep capped at {args.ref_iters} iterations",
+        "config": {"workload": f"standard deck {n}x{n}, tl_eps 1e-15, timesteps 1..{args.steps} "
+                               "after the warm-up timesteps",
+                   "method": f"CG + jac_diag, fp64 (the reference's method), each timestep capped at "
+                             f"{args.ref_iters} iterations",
                    "parallelism": "cpu", "cells": n * n},
-        "cpu_baseline": {"value": value, "unit": "cell-iters/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "plain-CG cell-iters/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} timesteps of the {n}^2 deck, {args.ref_iters} "
                                    "CG iterations each, CPU oracle (C, OpenMP)"},
-        "e2e": {"value": value, "unit": "cell-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": value, "unit": "plain-CG cell-iters/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------- ours
-def run_ours(args):
+def timed_solves(ch, stream, steps, torch):
+    """`steps` solves timed with CUDA events on the library stream; returns
+    (total ms, per-step ms, per-step solve infos)"""
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    infos = []
+    evs[0].record(stream)
+    for k in range(steps):
+        infos.append(ch.timestep())
+        evs[k + 1].record(stream)
+    evs[-1].synchronize()
+    per = [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)]
+    return evs[0].elapsed_time(evs[-1]), per, infos
+
+
+def load_model(ch, lib, path):
     import ctypes as C
 
     import numpy as np
+    from tealeaf_cuda_gb300 import learned
+    if not os.path.exists(path):
+        raise SystemExit(f"bench: warm start model {path} not found (train one with "
+                         "python -m tealeaf_cuda_gb300.learned train)")
+    p = np.ascontiguousarray(learned.load_model(path), dtype=np.float32)
+    if lib.tl_set_warm_start_model(ch._h, C.c_void_p(p.ctypes.data), p.size) != 0:
+        raise SystemExit("bench: tl_set_warm_start_model failed")
+
+
+def run_ours(args):
+    import ctypes as C
+
     import torch
 
     import tealeaf_cuda_gb300 as tl
@@ -239,45 +296,41 @@ def run_ours(args):
     rank, ws, local = dist_init()
     torch.cuda.set_device(local)
     lib = tl.load()
-    n = args.n
-    deck = make_deck(n, solver=args.solver, precond=args.precond, precision=args.precision)
-    cfg = tl.parse_deck(deck)
-    cfg.cuda_device = local
-    ch = tl.Chunk(cfg)
-    ch.start()
-    stream = torch.cuda.ExternalStream(lib.tl_chunk_stream(ch._h), device=local)
+    n, K = args.n, args.steps
     cells = n * n
 
+    # ---------------- headline method
+    cfg = tl.parse_deck(make_deck(n, solver=args.solver, precond=args.precond, precision=args.precision,
+                                  warm=args.warm))
+    cfg.cuda_device = local
+    ch = tl.Chunk(cfg)
+    if args.warm == "learned":
+        load_model(ch, lib, args.model)
+    stream = torch.cuda.ExternalStream(lib.tl_chunk_stream(ch._h), device=local)
+    ch.start()
     for _ in range(args.warmup):
         ch.timestep()
 
-    # ---- value: device-resident solves, CUDA events on the library stream
+    # ---- value: timesteps 1..K of a fresh run, device-resident
+    ch.start()
     barrier(ws)
     torch.cuda.synchronize()
     launches0 = ch.kernel_launches
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    its = []
     with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            its.append(ch.timestep()["iterations"])
-        e1.record(stream)
-        e1.synchronize()
+        ms, per_ms, infos = timed_solves(ch, stream, K, torch)
     torch.cuda.synchronize()
     barrier(ws)
-    ms = e0.elapsed_time(e1)
     launches = ch.kernel_launches - launches0
     clocks = clk.summary()
-    ms_max = allreduce_max(ms, ws, local)
-    total_cell_its = allreduce_sum(float(cells * sum(its)), ws, local)
-    value = total_cell_its / (ms_max * 1e-3)
+    summary_h = ch.field_summary()
+    its_h = [i["iterations"] for i in infos]
 
-    # ---- roofline: per-kernel CUDA events over K more solves
+    # ---- roofline: per-kernel CUDA events over the same K timesteps
+    ch.start()
     lib.tl_set_profiling(ch._h, 1)
     lib.tl_profile_reset(ch._h)
-    prof_its = 0
-    for _ in range(args.steps):
-        prof_its += ch.timestep()["iterations"]
+    for _ in range(K):
+        ch.timestep()
     kernels = {}
     k = 0
     while True:
@@ -291,8 +344,8 @@ def run_ours(args):
     total_kms = sum(v["ms"] for v in kernels.values()) or 1.0
     dom = max(kernels, key=lambda x: kernels[x]["ms"])
     dom_launch_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
-    bytes_per_launch = BYTES_PER_CELL.get(dom, 0) * cells
-    achieved = bytes_per_launch / (dom_launch_ms * 1e-3) / 1e9
+    bpc = bytes_per_cell(dom, args.precond)
+    achieved = (bpc or 0) * cells / (dom_launch_ms * 1e-3) / 1e9
     peaks = {}
     pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
@@ -303,56 +356,85 @@ def run_ours(args):
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_src,
                 "traffic": args.traffic_per_launch,
-                "bytes_per_cell": BYTES_PER_CELL.get(dom), "launch_ms": dom_launch_ms,
+                "bytes_per_cell": bpc, "launch_ms": dom_launch_ms,
                 "kernel_share": {k2: round(v["ms"] / total_kms, 4) for k2, v in
                                  sorted(kernels.items(), key=lambda kv: -kv[1]["ms"])},
-                "measured_over": f"{args.steps} solves, eager launches with per-kernel CUDA events"}
+                "measured_over": f"timesteps 1..{K}, eager launches with per-kernel CUDA events"}
 
-    # ---- e2e: host buffers through the C-ABI, copies inside the timed region
-    shape = ch.shape
-    host_rho = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-    host_e = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-    host_rho[:] = ch.get_field("density")
-    host_e[:] = ch.get_field("energy1")
-    h2d = 2 * host_rho.nbytes
+    # ---- e2e: the state lives on the host; every timestep uploads density
+    # and energy from pinned buffers, solves and reads energy back
+    ch.start()
+    pin = dict(dtype=torch.float64, pin_memory=True)
+    host_rho = torch.empty(ch.shape, **pin).numpy()
+    host_e = torch.empty(ch.shape, **pin).numpy()
+    ch.get_field("density", out=host_rho)
+    ch.get_field("energy1", out=host_e)
+    h2d = host_rho.nbytes + host_e.nbytes
     d2h = host_e.nbytes
     barrier(ws)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    e2e_its = 0
-    for _ in range(args.steps):
+    e2e_its = []
+    for _ in range(K):
         ch.set_field("density", host_rho)
         ch.set_field("energy1", host_e)
-        e2e_its += ch.timestep()["iterations"]
-        host_e[:] = ch.get_field("energy1")
+        e2e_its.append(ch.timestep()["iterations"])
+        ch.get_field("energy1", out=host_e)
     torch.cuda.synchronize()
     e2e_s = allreduce_max(time.perf_counter() - t0, ws, local)
-    e2e_total = allreduce_sum(float(cells * e2e_its), ws, local)
-    e2e = {"value": e2e_total / e2e_s, "unit": "cell-iters/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / args.steps}
     ch.close()
+
+    # ---------------- plain FP64 CG + jac_diag on the same timesteps
+    pcfg = tl.parse_deck(make_deck(n))
+    pcfg.cuda_device = local
+    pch = tl.Chunk(pcfg)
+    pstream = torch.cuda.ExternalStream(lib.tl_chunk_stream(pch._h), device=local)
+    pch.start()
+    barrier(ws)
+    torch.cuda.synchronize()
+    pms, pper_ms, pinfos = timed_solves(pch, pstream, K, torch)
+    summary_p = pch.field_summary()
+    pch.close()
+    its_p = [i["iterations"] for i in pinfos]
+
+    ms_max = allreduce_max(ms, ws, local)
+    work = allreduce_sum(float(cells * sum(its_p)), ws, local)
+    value = work / (ms_max * 1e-3)
+    e2e = {"value": work / e2e_s, "unit": "plain-CG cell-iters/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / K, "iterations_per_step": e2e_its}
+    rel = [abs(a - b) / abs(b) if b else abs(a) for a, b in zip(summary_h, summary_p)]
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        per, threads = oracle_sample(n, args.cpu_iters, 1)
+        cap = args.cpu_iters or max(50, min(3000, int(4e10 / cells)))
+        per, threads = oracle_sample(n, cap, 1)
         it0, w0 = per[0]
-        cpu = {"value": cells * it0 / w0, "unit": "cell-iters/s", "cores": threads, "kind": "port",
-               "sample": f"one timestep of the {n}^2 deck capped at {args.cpu_iters} CG+jac_diag "
-                         f"iterations ({it0} run, {w0:.1f} s), CPU oracle (C, OpenMP)"}
+        cpu = {"value": cells * it0 / w0, "unit": "plain-CG cell-iters/s", "cores": threads, "kind": "port",
+               "sample": f"timestep 1 of the {n}^2 deck by CG + jac_diag capped at {cap} iterations "
+                         f"({it0} run, {w0:.1f} s), CPU oracle (C, OpenMP)"}
 
     if rank == 0:
+        method = (f"{args.solver.upper()} + {args.precond}"
+                  + (" (10 inner steps)" if args.solver == "ppcg" else "")
+                  + f", {args.precision}, warm start {args.warm}")
         line = {
-            "metric": METRIC, "value": value, "unit": "cell-iters/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "metric": METRIC, "value": value, "unit": "plain-CG cell-iters/s", "n_gpus": ws,
+            "steps": K, "warmup": args.warmup, "ms_per_step": ms_max / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32+f64",
             "data": "synthetic (standard five-state deck of the reference benchmarks)",
-            "config": {"workload": f"standard deck {n}x{n}, {args.solver.upper()} + {args.precond}, "
-                                   f"{args.precision}, tl_eps 1e-15, one timestep per step",
-                       "cells": cells, "iterations_per_step": its,
-                       "time_to_solution_ms_per_step": ms_max / args.steps,
-                       "l2": "fields larger than L2 (134 MB each), no flush",
+            "config": {"workload": f"standard deck {n}x{n}, tl_eps 1e-15, timesteps 1..{K} of a fresh run",
+                       "method": method, "cells": cells,
+                       "iterations_per_step": its_h,
+                       "time_to_solution_ms": per_ms,
+                       "plain_method": "CG + jac_diag, fp64, u = u^n start",
+                       "plain_iterations_per_step": its_p,
+                       "plain_time_to_solution_ms": pper_ms,
+                       "time_to_solution_speedup_vs_plain": pms / ms,
+                       "field_summary_rel_diff_vs_plain": max(rel),
+                       "warm_used": [i.get("warm_used") for i in infos],
+                       "l2": "fields larger than L2, no flush",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches,
@@ -366,15 +448,17 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=4096)
-    ap.add_argument("--solver", default="cg", choices=["cg", "ppcg", "chebyshev"])
-    ap.add_argument("--precond", default="jac_diag", choices=["none", "jac_diag", "jac_block"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--ref-iters", type=int, default=200)
-    ap.add_argument("--cpu-iters", type=int, default=1500)
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--solver", default="ppcg", choices=["cg", "ppcg", "chebyshev"])
+    ap.add_argument("--precond", default="jac_block", choices=["none", "jac_diag", "jac_block"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--warm", default="learned", choices=["none", "prev", "learned"])
+    ap.add_argument("--model", default=DEFAULT_MODEL)
+    ap.add_argument("--ref-iters", type=int, default=100)
+    ap.add_argument("--cpu-iters", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-per-launch", type=float, default=None,
                     help="dram bytes per launch of the dominant kernel from an ncu capture")

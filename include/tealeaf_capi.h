@@ -61,6 +61,10 @@ extern "C" {
 /* numerical form of the solve (no reference counterpart) */
 #define TL_PRECISION_FP64        0  /* plain FP64: the drop-in               */
 #define TL_PRECISION_MIXED       1  /* FP32 inner Krylov + FP64 refinement   */
+/* start of the implicit solve (no reference counterpart; tl_warm_start) */
+#define TL_WARM_NONE             0  /* u = u^n, the reference's start        */
+#define TL_WARM_LEARNED          1  /* network + previous increment, Galerkin */
+#define TL_WARM_PREV             2  /* previous increment, Galerkin          */
 /* field ids: FIELD_* of data.f90:44-50 plus solver work arrays */
 #define TL_FIELD_DENSITY         1
 #define TL_FIELD_ENERGY0         2
@@ -111,7 +115,7 @@ typedef struct tl_config {
     int profiler_on, verbose, test_problem, cuda_device;
     int precision;                /* TL_PRECISION_* (tl_precision)           */
     double inner_eps;             /* mixed: inner FP32 relative tolerance    */
-    int warm_start;               /* 1: learned warm start (tl_warm_start)   */
+    int warm_start;               /* TL_WARM_* (tl_warm_start)               */
     int nstates;
     tl_state_t states[TL_MAX_STATES];
 } tl_config_t;
@@ -132,7 +136,7 @@ typedef struct tl_solve_info {
     double eigmin, eigmax;
     double rx, ry;
     double seconds;               /* wall time of the solve on the host      */
-    int warm_used;                /* learned start kept (1) or fell back (0) */
+    int warm_used;                /* warm start taken (1) or u = u^n (0)     */
     double warm_ratio;            /* its residual / the plain start's        */
 } tl_solve_info_t;
 
@@ -203,21 +207,29 @@ int tl_default_chunk_init(const tl_config_t *cfg);
 int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long pitch,
                    double *result, void *stream);
 
-/* ------------------------------------------------ learned warm start
- * No reference counterpart.  A residual network of six 3x3 convolutions
- * (32 channels, GELU, BF16 tensor-core kernels) predicts u^{n+1} - u^n from
- * (u^n, log density, Kx, Ky, dt); with cfg.warm_start set, tl_timestep starts
- * from u^n + du when that lowers the residual and from u^n otherwise, and
- * keeps the exit test tl_eps * (residual of the plain start).
+/* ------------------------------------------------ warm starts
+ * No reference counterpart.  With cfg.warm_start set, tl_timestep starts from
+ *   u = u^n + a d_net + b d_prev
+ * where d_prev = u^n - u^{n-1} (the previous step's increment; absent on the
+ * first step after tl_start) and d_net is a residual network's prediction of
+ * the correction A^-1 (u^n - A u^n) (TL_WARM_LEARNED only).  (a, b) solve the
+ * 2x2 Galerkin system that minimises the energy 1/2 u.Au - u.u^n, so the
+ * start's A-norm error is never above the plain start's; the exit test stays
+ * tl_eps * (residual of the plain start u = u^n).
  *
- * Parameters: FP32, flat, per layer W[9][coutp][cin] then b[coutp]; layers
- * (cin, coutp) = (16,32) GELU, 4 x (32,32) x + GELU(conv x), (32,16) linear
- * head (output channel 0).  A model file is the 8 bytes "TLWS0001", an
- * int64 parameter count, then the FP32 parameters. */
+ * The network: six 3x3 convolutions (32 channels, GELU, BF16 tensor-core
+ * kernels).  Inputs per cell: u^n/max|u^n|, log density, log1p Kx, log1p Ky,
+ * 100 dt, r0/max|r0|, d_prev/max|r0| (r0 = u^n - A u^n); output: the
+ * correction / max|r0|.  Parameters: FP32, flat, per layer W[9][coutp][cin]
+ * then b[coutp]; layers (cin, coutp) = (16,32) GELU, 4 x (32,32)
+ * x + GELU(conv x), (32,16) linear head (output channel 0).  A model file is
+ * the 8 bytes "TLWS0001", an int64 parameter count, then the FP32
+ * parameters. */
 long long tl_warm_start_param_count(void);
 int tl_set_warm_start_model(tl_chunk_t *ch, const float *params, long long n);
-/* training data of the step just solved: FP32 [ny][nx][6] at device dst =
- * (u^n/s, log density, log1p Kx, log1p Ky, 100 dt, (u^{n+1}-u^n)/s), s = max|u^n| */
+/* training data of the step just solved (which must have run with a warm
+ * start, so that u^{n-1} is tracked): FP32 [ny][nx][8] at device dst = the
+ * seven network inputs and the target (u^{n+1} - u^n)/max|r0| */
 int tl_warm_start_features(tl_chunk_t *ch, float *dst);
 
 /* Network kernels on caller-owned device buffers (NHWC BF16 activations with

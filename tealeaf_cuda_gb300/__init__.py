@@ -25,6 +25,7 @@ TL_ERR_STATE, TL_ERR_DECK, TL_ERR_EIGEN = -5, -6, -7
 SOLVER_JACOBI, SOLVER_CG, SOLVER_CHEBYSHEV, SOLVER_PPCG = 1, 2, 3, 4
 PREC_NONE, PREC_JAC_DIAG, PREC_JAC_BLOCK = 1, 2, 3
 PRECISION_FP64, PRECISION_MIXED = 0, 1
+WARM_NONE, WARM_LEARNED, WARM_PREV = 0, 1, 2
 FIELDS = {"density": 1, "energy0": 2, "energy1": 3, "u": 4, "p": 5, "sd": 6, "r": 7,
           "u0": 8, "w": 9, "z": 10, "kx": 11, "ky": 12, "mi": 13, "cp": 14, "bfp": 15,
           "volume": 16, "rtemp": 17, "utemp": 18, "r_store": 19}
@@ -254,8 +255,11 @@ class Chunk:
         _check(load().tl_field_summary(self._h, *[C.byref(x) for x in v]), "tl_field_summary")
         return tuple(x.value for x in v)
 
-    def get_field(self, name):
-        a = np.empty(self.shape, dtype=np.float64)
+    def get_field(self, name, out=None):
+        """the whole padded field (device -> host); into `out` (C-contiguous
+        float64 of self.shape, e.g. pinned) when given"""
+        a = np.empty(self.shape, dtype=np.float64) if out is None else out
+        assert a.shape == self.shape and a.dtype == np.float64 and a.flags.c_contiguous
         _check(load().tl_get_field(self._h, FIELDS[name], a.ctypes.data), "tl_get_field")
         return a
 

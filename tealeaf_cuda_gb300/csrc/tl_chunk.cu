@@ -411,6 +411,11 @@ int tl_start(tl_chunk_t *ch, double *vol, double *mass, double *ie, double *temp
     if ((rc = chunk_update_halo(c, fl, c->h))) return rc;
     if ((rc = launch_set_field(c))) return rc;
     c->dt = cf.dtinit;
+    // a (re)start begins a fresh run: the tea_solve.f90 SAVE state (first
+    // solve, eigenvalue estimates) and the warm start's u^(n-1) are reset
+    c->first = true;
+    c->eigmin = c->eigmax = c->theta = c->cn = 0.0;
+    warm_reset(c);
     return field_summary(c, vol, mass, ie, temp);
 }
 

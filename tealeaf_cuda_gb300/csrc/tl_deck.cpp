@@ -227,8 +227,9 @@ void parse(const char *text, tl_config_t *c) {
             else if (w == "tl_inner_eps") c->inner_eps = d.rval();
             else if (w == "tl_warm_start") {
                 std::string v = d.word(true);
-                if (v == "none" || v == "prev") c->warm_start = 0;
-                else if (v == "learned") c->warm_start = 1;
+                if (v == "none") c->warm_start = TL_WARM_NONE;
+                else if (v == "prev") c->warm_start = TL_WARM_PREV;
+                else if (v == "learned") c->warm_start = TL_WARM_LEARNED;
                 else throw DeckError{TL_ERR_DECK, "Invalid tl_warm_start: " + v};
             }
             else if (w == "state") {

@@ -355,7 +355,7 @@ extern "C" int tl_run_deck(const char *deck_text, const tl_run_options_t *opt, t
     } else {
         rc = tl_chunk_create(&cf, &ch);
         if (!rc) rc = tl_start(ch, &vol, &mass, &ie, &temp);
-        if (!rc && cf.warm_start) rc = load_model(ch, o.model_path);
+        if (!rc && cf.warm_start == TL_WARM_LEARNED) rc = load_model(ch, o.model_path);
     }
     if (rc) {
         fprintf(stderr, "tea_leaf: start failed: %s\n", tl_last_error());

@@ -212,15 +212,15 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
 int mixed_ppcg_prepare(Chunk *c);  // FP32 operator + preconditioner copies
 int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
-// learned warm start (tl_warm.cu)
+// warm starts (tl_warm.cu)
 void warm_free(Chunk *c);
+void warm_reset(Chunk *c);                // forget u^(n-1) (tl_start)
 long long warm_param_count();
 int warm_set_model(Chunk *c, const float *params, long long n);
-bool warm_ready(Chunk *c);
-int warm_apply(Chunk *c);                 // u = u0 + du after common_init
-int warm_features(Chunk *c, float *dst);  // [ny][nx][6] features + target
-// learned start with fallback: after common_init, sets u and r, returns the
-// plain start's residual norm r0 in *r0 and the chosen start's r.r in *rr
+bool warm_ready(Chunk *c);                // a network is loaded
+int warm_features(Chunk *c, float *dst);  // [ny][nx][8] inputs + target
+// Galerkin warm start after common_init: sets u and r, returns the plain
+// start's residual norm in *r0 and the chosen start's r.r in *rr
 int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *rr);
 
 }  // namespace tl

@@ -440,106 +440,105 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
     float4 xm = live ? ld4(sd_in, i - P) : z4;
     float4 x0 = live ? ld4(sd_in, i) : z4;
     float4 ky0 = live ? ld4(ky, i) : z4;
+    // sd = alpha sd + beta z; utemp += sd; store (z64 on the last step)
+    auto finish = [&](int64_t ik, int row, float4 sdo, float4 zv) {
+        if (nv <= 0) return;
+        float4 sn;
+        sn.x = fmaf(al, sdo.x, be * zv.x);
+        sn.y = fmaf(al, sdo.y, be * zv.y);
+        sn.z = fmaf(al, sdo.z, be * zv.z);
+        sn.w = fmaf(al, sdo.w, be * zv.w);
+        const float4 ut = ld4(utemp, ik);
+        const float4 un = make_float4(ut.x + sn.x, ut.y + sn.y, ut.z + sn.z, ut.w + sn.w);
+        if (LAST) {
+            const int64_t i64 = (int64_t)(c + g.h) + (int64_t)(row + g.h) * pitch64;
+            const float *uq = &un.x;
+            for (int q = 0; q < nv; ++q) z64[i64 + q] = (double)uq[q];
+        } else {
+            st4(sd_out, ik, sn, nv);
+            st4(utemp, ik, un, nv);
+        }
+    };
+    // rtemp - A sd for the row at ik (advances the row window)
+    auto stencil_row = [&](int64_t ik) {
+        const float4 xp = live ? ld4(sd_in, ik + P) : z4;
+        const float4 ky1 = live ? ld4(ky, ik + P) : z4;
+        const float4 kxv = live ? ld4(kx, ik) : z4;
+        float kxe = __shfl_down_sync(0xffffffffu, kxv.x, 1);
+        float xe = __shfl_down_sync(0xffffffffu, x0.x, 1);
+        float xw = __shfl_up_sync(0xffffffffu, x0.w, 1);
+        if (lane == 31 && live) {
+            kxe = kx[ik + 4];
+            xe = sd_in[ik + 4];
+        }
+        if (lane == 0 && live) xw = sd_in[ik - 1];
+        const float4 r0 = live ? ld4(rtemp, ik) : z4;
+        float4 o;
+        o.x = r0.x - cell_apply(x0.x, xp.x, xm.x, xw, x0.y, ky1.x, ky0.x, kxv.y, kxv.x);
+        o.y = r0.y - cell_apply(x0.y, xp.y, xm.y, x0.x, x0.z, ky1.y, ky0.y, kxv.z, kxv.y);
+        o.z = r0.z - cell_apply(x0.z, xp.z, xm.z, x0.y, x0.w, ky1.z, ky0.z, kxv.w, kxv.z);
+        o.w = r0.w - cell_apply(x0.w, xp.w, xm.w, x0.z, xe, ky1.w, ky0.w, kxe, kxv.w);
+        xm = x0;
+        x0 = xp;
+        ky0 = ky1;
+        if (!LAST) st4(rtemp, ik, o, nv);
+        return o;
+    };
+    if constexpr (PC != TL_PREC_JAC_BLOCK) {
+        // pointwise preconditioner: finish each row as soon as it is computed
+#pragma unroll
+        for (int rr = 0; rr < kVRows; ++rr) {
+            if (j0 + rr >= g.ny) break;
+            const int64_t ik = i + (int64_t)rr * P;
+            const float4 sdo = x0;
+            const float4 rt = stencil_row(ik);
+            float4 zv = rt;
+            if (PC == TL_PREC_JAC_DIAG) {
+                const float4 mv = live ? ld4(mi, ik) : z4;
+                zv = make_float4(rt.x * mv.x, rt.y * mv.y, rt.z * mv.z, rt.w * mv.w);
+            }
+            finish(ik, j0 + rr, sdo, zv);
+        }
+    } else {
 #pragma unroll
     for (int s0 = 0; s0 < kVRows; s0 += 4) {
         if (j0 + s0 >= g.ny) break;
         const int m = min(4, g.ny - (j0 + s0));
-        float4 rt[4], sv[4];
+        // rtemp of the strip's rows, then z = M^-1 rtemp in place (Thomas:
+        // dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k, z_k = dp_k - cp_k z_{k+1})
+        float4 v[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (k >= m) break;
             const int64_t ik = i + (int64_t)(s0 + k) * P;
-            const float4 xp = live ? ld4(sd_in, ik + P) : z4;
-            const float4 ky1 = live ? ld4(ky, ik + P) : z4;
-            const float4 kxv = live ? ld4(kx, ik) : z4;
-            float kxe = __shfl_down_sync(0xffffffffu, kxv.x, 1);
-            float xe = __shfl_down_sync(0xffffffffu, x0.x, 1);
-            float xw = __shfl_up_sync(0xffffffffu, x0.w, 1);
-            if (lane == 31 && live) {
-                kxe = kx[ik + 4];
-                xe = sd_in[ik + 4];
-            }
-            if (lane == 0 && live) xw = sd_in[ik - 1];
-            const float4 r0 = live ? ld4(rtemp, ik) : z4;
-            float4 o;
-            o.x = r0.x - cell_apply(x0.x, xp.x, xm.x, xw, x0.y, ky1.x, ky0.x, kxv.y, kxv.x);
-            o.y = r0.y - cell_apply(x0.y, xp.y, xm.y, x0.x, x0.z, ky1.y, ky0.y, kxv.z, kxv.y);
-            o.z = r0.z - cell_apply(x0.z, xp.z, xm.z, x0.y, x0.w, ky1.z, ky0.z, kxv.w, kxv.z);
-            o.w = r0.w - cell_apply(x0.w, xp.w, xm.w, x0.z, xe, ky1.w, ky0.w, kxe, kxv.w);
-            rt[k] = o;
-            sv[k] = x0;
-            xm = x0;
-            x0 = xp;
-            ky0 = ky1;
-        }
-        // z = M^-1 rtemp for the strip
-        float4 zz[4];
-        if (PC == TL_PREC_JAC_BLOCK) {
-            // forward sweep: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k
-            float4 dp[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (k >= m) break;
-                const int64_t ik = i + (int64_t)(s0 + k) * P;
-                const float4 bf = live ? ld4(bfp, ik) : z4;
-                if (k == 0) {
-                    dp[0] = make_float4(rt[0].x * bf.x, rt[0].y * bf.y, rt[0].z * bf.z, rt[0].w * bf.w);
-                } else {
-                    const float4 kyk = live ? ld4(ky, ik) : z4;
-                    dp[k].x = fmaf(kyk.x, dp[k - 1].x, rt[k].x) * bf.x;
-                    dp[k].y = fmaf(kyk.y, dp[k - 1].y, rt[k].y) * bf.y;
-                    dp[k].z = fmaf(kyk.z, dp[k - 1].z, rt[k].z) * bf.z;
-                    dp[k].w = fmaf(kyk.w, dp[k - 1].w, rt[k].w) * bf.w;
-                }
-            }
-#pragma unroll
-            for (int k = 3; k >= 0; --k) {
-                if (k >= m) continue;
-                if (k == m - 1) {
-                    zz[k] = dp[k];
-                } else {
-                    const float4 cv = live ? ld4(cp, i + (int64_t)(s0 + k) * P) : z4;
-                    zz[k].x = fmaf(-cv.x, zz[k + 1].x, dp[k].x);
-                    zz[k].y = fmaf(-cv.y, zz[k + 1].y, dp[k].y);
-                    zz[k].z = fmaf(-cv.z, zz[k + 1].z, dp[k].z);
-                    zz[k].w = fmaf(-cv.w, zz[k + 1].w, dp[k].w);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (k >= m) break;
-                if (PC == TL_PREC_JAC_DIAG) {
-                    const float4 mv = live ? ld4(mi, i + (int64_t)(s0 + k) * P) : z4;
-                    zz[k] = make_float4(rt[k].x * mv.x, rt[k].y * mv.y, rt[k].z * mv.z, rt[k].w * mv.w);
-                } else {
-                    zz[k] = rt[k];
-                }
-            }
-        }
-        // sd = alpha sd + beta z; utemp += sd
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (k >= m) break;
-            const int64_t ik = i + (int64_t)(s0 + k) * P;
-            if (nv <= 0) continue;
-            float4 sn;
-            sn.x = fmaf(al, sv[k].x, be * zz[k].x);
-            sn.y = fmaf(al, sv[k].y, be * zz[k].y);
-            sn.z = fmaf(al, sv[k].z, be * zz[k].z);
-            sn.w = fmaf(al, sv[k].w, be * zz[k].w);
-            const float4 ut = ld4(utemp, ik);
-            const float4 un = make_float4(ut.x + sn.x, ut.y + sn.y, ut.z + sn.z, ut.w + sn.w);
-            if (LAST) {
-                const int64_t i64 = (int64_t)(c + g.h) + (int64_t)(j0 + s0 + k + g.h) * pitch64;
-                const float *uq = &un.x;
-                for (int q = 0; q < nv; ++q) z64[i64 + q] = (double)uq[q];
+            const float4 kyk = ky0;  // the face below row k, before the window moves
+            const float4 rt = stencil_row(ik);
+            const float4 bf = live ? ld4(bfp, ik) : z4;
+            if (k == 0) {
+                v[0] = make_float4(rt.x * bf.x, rt.y * bf.y, rt.z * bf.z, rt.w * bf.w);
             } else {
-                st4(rtemp, ik, rt[k], nv);
-                st4(sd_out, ik, sn, nv);
-                st4(utemp, ik, un, nv);
+                v[k].x = fmaf(kyk.x, v[k - 1].x, rt.x) * bf.x;
+                v[k].y = fmaf(kyk.y, v[k - 1].y, rt.y) * bf.y;
+                v[k].z = fmaf(kyk.z, v[k - 1].z, rt.z) * bf.z;
+                v[k].w = fmaf(kyk.w, v[k - 1].w, rt.w) * bf.w;
             }
         }
+#pragma unroll
+        for (int k = 2; k >= 0; --k) {
+            if (k >= m - 1) continue;
+            const float4 cv = live ? ld4(cp, i + (int64_t)(s0 + k) * P) : z4;
+            v[k].x = fmaf(-cv.x, v[k + 1].x, v[k].x);
+            v[k].y = fmaf(-cv.y, v[k + 1].y, v[k].y);
+            v[k].z = fmaf(-cv.z, v[k + 1].z, v[k].z);
+            v[k].w = fmaf(-cv.w, v[k + 1].w, v[k].w);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (k >= m) break;
+            const int64_t ik = i + (int64_t)(s0 + k) * P;
+            finish(ik, j0 + s0 + k, live ? ld4(sd_in, ik) : z4, v[k]);
+        }
+    }
     }
 }
 
@@ -802,8 +801,8 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
     if ((rc = chunk_push_scalars(c))) return rc;
     double r0, rn;
     if (cf.warm_start) {
-        // learned start or the plain one, whichever has the smaller residual;
-        // the target stays tl_eps times the plain start's residual
+        // Galerkin warm start; the target stays tl_eps times the plain
+        // start's residual
         double rr = 0.0;
         if ((rc = warm_start_or_fallback(c, info, &r0, &rr))) return rc;
         rn = sqrt(fabs(rr));

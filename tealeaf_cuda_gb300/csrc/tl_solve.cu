@@ -189,8 +189,8 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info) {
     if ((rc = halo(c, TL_FIELD_U, 1))) return rc;
 
     // scalars of this solve
-    // learned warm start: u = u^n + du if that lowers the residual, else the
-    // plain start; the exit test keeps the plain start's residual
+    // warm start: u = u^n + the Galerkin combination of the network's and the
+    // previous step's directions; the exit test keeps the plain start's residual
     double warm_r0 = 0.0, warm_rr = 0.0;
     const bool warm = cf.warm_start != 0;
     if (warm && (rc = warm_start_or_fallback(c, info, &warm_r0, &warm_rr))) return rc;

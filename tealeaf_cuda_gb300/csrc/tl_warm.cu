@@ -1,13 +1,27 @@
-// tl_warm.cu -- the learned warm start inside the solve (no reference
-// counterpart): features of the current step, the residual network's
-// forward pass on the tensor-core kernels of tl_conv.cu, and u = u^n + du.
-// The solve compares the residual of this start with that of the plain
-// start u = u^n and keeps the better one (the fallback); its exit test stays
-// tl_eps times the plain start's residual.
+// tl_warm.cu -- warm starts of the implicit solve (no reference counterpart).
+//
+// The system of a timestep is A u = u^n with A = I + the Kx/Ky stencil
+// (tea_leaf_common.cuknl:28-34); the plain start is u = u^n, whose residual
+// is r0 = u^n - A u^n, and the exact correction is du = A^-1 r0.  A warm
+// start adds a combination of search directions to u^n:
+//   d_net  = the residual network's prediction of du (tl_warm_start learned)
+//   d_prev = u^n - u^(n-1), the previous step's increment (both modes)
+// with the coefficients that minimise the energy
+//   phi(u) = 1/2 u.Au - u.u^n   over   u = u^n + a d_net + b d_prev,
+// i.e. the 2x2 Galerkin system [d.Ad'] (a, b) = [d.r0].  Because A is SPD,
+// phi - phi(u*) = 1/2 |u - u*|_A^2, so the chosen start never has a larger
+// A-norm error than the plain one.  The solve's exit test stays tl_eps times
+// the plain start's residual, so the answer meets the same tolerance.
+//
+// Network input per cell (channels 0..6, BF16, NHWC, 1-pixel zero halo):
+//   u^n / max|u^n|, log density, log1p(Kx west face), log1p(Ky south face),
+//   100 dt, r0 / max|r0|, d_prev / max|r0|;
+// output channel 0 is du / max|r0| (the network is linear-equivariant in the
+// residual's scale).
 //
 // Model parameters (FP32, flat, in this order per layer: W [9][coutp][cin]
 // then b [coutp]):
-//   layer 1: cin 16 (inputs 0..4 used), coutp 32, GELU
+//   layer 1: cin 16 (inputs 0..6 used), coutp 32, GELU
 //   layers 2-5: cin 32, coutp 32, x + GELU(conv x)
 //   layer 6: cin 32, coutp 16 (output channel 0 used), linear head
 #include <cuda_bf16.h>
@@ -32,167 +46,267 @@ using bf16 = __nv_bfloat16;
 constexpr int kLayers = 6;
 constexpr int kCin[kLayers] = {16, 32, 32, 32, 32, 32};
 constexpr int kCout[kLayers] = {32, 32, 32, 32, 32, 16};
+constexpr int kInputs = 7;          // network input channels in use
+constexpr int kFeatures = kInputs + 1;  // + the training target
+constexpr int kGramBlocks = 608;    // 152 SMs x 4
+constexpr int kGramSums = 6;        // Gnn, Gnp, Gpp, bn, bp, r0.r0
+constexpr float kClamp = 64.f;      // bound of the scaled inputs
 
 struct Warm {
+    // previous-step tracking (both warm start modes)
+    double *uprev;              // u^(n-1), field layout
+    double *dprev;              // u^n - u^(n-1) of the current step
+    double *dnet;               // network direction (field layout, zero halo)
+    double *r0;                 // scratch: u^n - A u^n
+    double *partials;           // [kGramBlocks][kGramSums]
+    float *scale;               // device [0] max|u^n|, [1] max|r0|
+    bool have_prev;
+    std::vector<void *> allocs;
+    // the network (learned mode)
+    bool model;
     float *params;              // FP32 master copy on the device
     bf16 *wf[kLayers];          // BF16 [9][coutp][cin]
     float *bias[kLayers];
     bf16 *x, *h0, *h1, *pre;    // activations [1][ny+2][nxp+2][C]
-    float *y;                   // [ny][nxp] predicted du / s
-    float *scale;               // device max |u0|
+    float *y;                   // [ny][nxp] predicted du / max|r0|
     int nxp;
-    std::vector<void *> allocs;
+    std::vector<void *> model_allocs;
 };
 
 long long layer_floats(int l) { return 9LL * kCin[l] * kCout[l] + kCout[l]; }
 
-// max |u0| over the interior (non-negative floats compare as unsigned ints)
-__global__ void k_absmax(Geo g, const double *__restrict__ u0, float *__restrict__ out) {
-    float m = 0.f;
+__device__ __forceinline__ int64_t cell_of(const Geo &g, long long k, int *i, int *j) {
+    *i = (int)(k % g.nx);
+    *j = (int)(k / g.nx);
+    return (int64_t)(*i + g.h) + (int64_t)(*j + g.h) * g.pitch;
+}
+
+// (A v)[c]: the operator of tea_leaf_common.cuknl:28-34 with the stored diagonal
+__device__ __forceinline__ double apply_a(const double *__restrict__ v, const double *__restrict__ dg,
+                                          const double *__restrict__ kx, const double *__restrict__ ky,
+                                          int64_t c, int pitch) {
+    const double a = fma(ky[c + pitch], v[c + pitch], ky[c] * v[c - pitch]);
+    const double b = fma(kx[c + 1], v[c + 1], kx[c] * v[c - 1]);
+    return fma(dg[c], v[c], -a) - b;
+}
+
+// out[0] = max |a|, out[1] = max |b| over the interior (b may be null);
+// non-negative floats compare as unsigned ints
+__global__ void k_absmax2(Geo g, const double *__restrict__ a, const double *__restrict__ b,
+                          float *__restrict__ out) {
+    float ma = 0.f, mb = 0.f;
     const long long n = (long long)g.nx * g.ny;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(k % g.nx), j = (int)(k / g.nx);
-        m = fmaxf(m, (float)fabs(u0[(int64_t)(i + g.h) + (int64_t)(j + g.h) * g.pitch]));
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        ma = fmaxf(ma, (float)fabs(a[c]));
+        if (b) mb = fmaxf(mb, (float)fabs(b[c]));
     }
-    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
-    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned int *>(out), __float_as_uint(m));
+    for (int off = 16; off > 0; off >>= 1) {
+        ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, off));
+        mb = fmaxf(mb, __shfl_xor_sync(0xffffffffu, mb, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(reinterpret_cast<unsigned int *>(out), __float_as_uint(ma));
+        atomicMax(reinterpret_cast<unsigned int *>(out + 1), __float_as_uint(mb));
+    }
 }
 
-// features of cell (i, j): u0 / s, log density, log1p(Kx west face),
-// log1p(Ky south face), 100 dt; written as BF16 into the padded NHWC input
-// (x != nullptr) and/or as FP32 [ny][nx][6] with the target (u - u0) / s
-// (f != nullptr)
+// r0 = u0 - A u0 on the interior
+__global__ void k_resid0(Geo g, const double *__restrict__ u0, const double *__restrict__ dg,
+                         const double *__restrict__ kx, const double *__restrict__ ky, double *__restrict__ r0) {
+    const long long n = (long long)g.nx * g.ny;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        r0[c] = u0[c] - apply_a(u0, dg, kx, ky, c, g.pitch);
+    }
+}
+
+// dprev = u0 - uprev (zero without a previous step); uprev = u0
+__global__ void k_prev(Geo g, const double *__restrict__ u0, double *__restrict__ uprev,
+                       double *__restrict__ dprev, int have) {
+    const long long n = (long long)g.nx * g.ny;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        const double v = u0[c];
+        dprev[c] = have ? v - uprev[c] : 0.0;
+        uprev[c] = v;
+    }
+}
+
+__device__ __forceinline__ float clampf(float v) { return fminf(fmaxf(v, -kClamp), kClamp); }
+
+// network inputs of cell (i, j), as BF16 into the padded NHWC input
+// (x != nullptr) and/or as FP32 [ny][nx][kFeatures] with the target
+// (u - u0) / max|r0| (f != nullptr)
 __global__ void k_features(Geo g, const double *__restrict__ u0, const double *__restrict__ u,
+                           const double *__restrict__ r0, const double *__restrict__ dprev,
                            const double *__restrict__ density, const double *__restrict__ kx,
                            const double *__restrict__ ky, const float *__restrict__ scale, double dt,
                            bf16 *__restrict__ x, int nxp, float *__restrict__ f) {
     const long long n = (long long)g.nx * g.ny;
-    const float s = fmaxf(*scale, 1e-30f);
+    const double su = fmax((double)scale[0], 1e-300), sr = fmax((double)scale[1], 1e-300);
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(k % g.nx), j = (int)(k / g.nx);
-        const int64_t c = (int64_t)(i + g.h) + (int64_t)(j + g.h) * g.pitch;
-        float v[5];
-        v[0] = (float)(u0[c] / s);
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        float v[kInputs];
+        v[0] = (float)(u0[c] / su);
         v[1] = logf((float)density[c]);
         v[2] = log1pf((float)kx[c]);
         v[3] = log1pf((float)ky[c]);
         v[4] = (float)(100.0 * dt);
+        v[5] = clampf((float)(r0[c] / sr));
+        v[6] = clampf((float)(dprev[c] / sr));
         if (x) {
             bf16 *d = x + (((int64_t)(j + 1)) * (nxp + 2) + i + 1) * 16;
-            for (int q = 0; q < 5; ++q) d[q] = __float2bfloat16(v[q]);
+            for (int q = 0; q < kInputs; ++q) d[q] = __float2bfloat16(v[q]);
         }
         if (f) {
-            float *d = f + k * 6;
-            for (int q = 0; q < 5; ++q) d[q] = v[q];
-            d[5] = (float)((u[c] - u0[c]) / s);
+            float *d = f + k * kFeatures;
+            for (int q = 0; q < kInputs; ++q) d[q] = v[q];
+            d[kInputs] = (float)((u[c] - u0[c]) / sr);
         }
     }
 }
 
-// u = u0 + s * du on the interior
-__global__ void k_apply(Geo g, const double *__restrict__ u0, double *__restrict__ u, const float *__restrict__ du,
-                        int nxp, const float *__restrict__ scale) {
+// dnet = max|r0| * y on the interior (the halo stays zero)
+__global__ void k_dnet(Geo g, const float *__restrict__ y, int nxp, const float *__restrict__ scale,
+                       double *__restrict__ dnet) {
     const long long n = (long long)g.nx * g.ny;
-    const double s = (double)fmaxf(*scale, 1e-30f);
+    const double sr = (double)scale[1];
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(k % g.nx), j = (int)(k / g.nx);
-        const int64_t c = (int64_t)(i + g.h) + (int64_t)(j + g.h) * g.pitch;
-        u[c] = u0[c] + s * (double)du[(int64_t)j * nxp + i];
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        dnet[c] = sr * (double)y[(int64_t)j * nxp + i];
+    }
+}
+
+// Gram entries of the Galerkin system, per CTA in a fixed order:
+// [dn.Adn, dn.Adp, dp.Adp, dn.r0, dp.r0, r0.r0]; a null direction counts 0
+__global__ void __launch_bounds__(256) k_gram(Geo g, const double *__restrict__ dn,
+                                              const double *__restrict__ dp, const double *__restrict__ r0,
+                                              const double *__restrict__ dg, const double *__restrict__ kx,
+                                              const double *__restrict__ ky, double *__restrict__ partials) {
+    double s[kGramSums] = {0, 0, 0, 0, 0, 0};
+    const long long n = (long long)g.nx * g.ny;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        const double r = r0[c];
+        s[5] = fma(r, r, s[5]);
+        if (dn) {
+            const double an = apply_a(dn, dg, kx, ky, c, g.pitch);
+            s[0] = fma(dn[c], an, s[0]);
+            s[3] = fma(dn[c], r, s[3]);
+            if (dp) s[1] = fma(dp[c], an, s[1]);
+        }
+        if (dp) {
+            const double ap = apply_a(dp, dg, kx, ky, c, g.pitch);
+            s[2] = fma(dp[c], ap, s[2]);
+            s[4] = fma(dp[c], r, s[4]);
+        }
+    }
+    __shared__ double red[8][kGramSums];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < kGramSums; ++q) {
+        double v = s[q];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kGramSums) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += red[w][threadIdx.x];
+        partials[(int64_t)blockIdx.x * kGramSums + threadIdx.x] = t;
+    }
+}
+
+// u = u0 + a dn + b dp on the interior
+__global__ void k_combine(Geo g, const double *__restrict__ u0, const double *__restrict__ dn, double a,
+                          const double *__restrict__ dp, double b, double *__restrict__ u) {
+    const long long n = (long long)g.nx * g.ny;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int i, j;
+        const int64_t c = cell_of(g, k, &i, &j);
+        double v = u0[c];
+        if (dn) v = fma(a, dn[c], v);
+        if (dp) v = fma(b, dp[c], v);
+        u[c] = v;
     }
 }
 
 Warm *warm_of(Chunk *c) { return (Warm *)c->warm; }
 
-int dmalloc(Warm *w, void **p, size_t bytes, cudaStream_t s) {
+int dmalloc(std::vector<void *> &list, void **p, size_t bytes, cudaStream_t s) {
     cudaError_t e = cudaMalloc(p, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "warm start cudaMalloc");
-    w->allocs.push_back(*p);
+    list.push_back(*p);
     e = cudaMemsetAsync(*p, 0, bytes, s);
     return e == cudaSuccess ? TL_OK : cuda_fail(e, "warm start memset");
 }
 
-}  // namespace
-
-void warm_free(Chunk *c) {
-    Warm *w = warm_of(c);
-    if (!w) return;
-    for (void *p : w->allocs) cudaFree(p);
-    delete w;
-    c->warm = nullptr;
+int launched(Chunk *c, const char *what, int n = 1) {
+    c->launches += n;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TL_OK : cuda_fail(e, what);
 }
 
-long long warm_param_count() {
-    long long n = 0;
-    for (int l = 0; l < kLayers; ++l) n += layer_floats(l);
-    return n;
+void free_model(Warm *w) {
+    for (void *p : w->model_allocs) cudaFree(p);
+    w->model_allocs.clear();
+    w->model = false;
 }
 
-int warm_set_model(Chunk *c, const float *params, long long n) {
-    if (n != warm_param_count()) {
-        set_error("warm start model: %lld parameters, expected %lld", n, warm_param_count());
-        return TL_ERR_ARG;
+// the per-chunk warm start state, created on first use
+int warm_state(Chunk *c, Warm **out) {
+    if (c->warm) {
+        *out = warm_of(c);
+        return TL_OK;
     }
-    warm_free(c);
     Warm *w = new Warm();
     c->warm = w;
+    const size_t bytes = sizeof(double) * c->alloc_elems;
+    const int64_t off = c->lead;  // field pointers start `lead` elements into the allocation
     cudaStream_t s = c->stream;
     int rc;
     void *p;
-    if ((rc = dmalloc(w, &p, sizeof(float) * n, s))) return rc;
-    w->params = (float *)p;
-    TL_CUDA(cudaMemcpyAsync(w->params, params, sizeof(float) * n, cudaMemcpyHostToDevice, s));
-    long long off = 0;
-    for (int l = 0; l < kLayers; ++l) {
-        if ((rc = dmalloc(w, &p, sizeof(bf16) * 9 * kCin[l] * kCout[l], s))) return rc;
-        w->wf[l] = (bf16 *)p;
-        if ((rc = tl_nn_pack(w->params + off, w->wf[l], nullptr, kCin[l], kCout[l], s))) return rc;
-        w->bias[l] = w->params + off + 9LL * kCin[l] * kCout[l];
-        off += layer_floats(l);
+    double **fields[4] = {&w->uprev, &w->dprev, &w->dnet, &w->r0};
+    for (double **f : fields) {
+        if ((rc = dmalloc(w->allocs, &p, bytes, s))) return rc;
+        *f = (double *)p + off;
     }
-    w->nxp = (c->nx + 15) / 16 * 16;
-    const size_t px = (size_t)(c->ny + 2) * (w->nxp + 2);
-    if ((rc = dmalloc(w, &p, sizeof(bf16) * px * 16, s))) return rc;
-    w->x = (bf16 *)p;
-    if ((rc = dmalloc(w, &p, sizeof(bf16) * px * 32, s))) return rc;
-    w->h0 = (bf16 *)p;
-    if ((rc = dmalloc(w, &p, sizeof(bf16) * px * 32, s))) return rc;
-    w->h1 = (bf16 *)p;
-    if ((rc = dmalloc(w, &p, sizeof(bf16) * px * 32, s))) return rc;
-    w->pre = (bf16 *)p;
-    if ((rc = dmalloc(w, &p, sizeof(float) * (size_t)c->ny * w->nxp, s))) return rc;
-    w->y = (float *)p;
-    if ((rc = dmalloc(w, &p, 256, s))) return rc;
+    if ((rc = dmalloc(w->allocs, &p, sizeof(double) * kGramBlocks * kGramSums, s))) return rc;
+    w->partials = (double *)p;
+    if ((rc = dmalloc(w->allocs, &p, 256, s))) return rc;
     w->scale = (float *)p;
-    TL_CUDA(cudaStreamSynchronize(s));
+    *out = w;
     return TL_OK;
 }
 
-bool warm_ready(Chunk *c) { return warm_of(c) != nullptr; }
-
-int warm_scale(Chunk *c, float *scale_dev) {
-    TL_CUDA(cudaMemsetAsync(scale_dev, 0, sizeof(float), c->stream));
-    k_absmax<<<608, 256, 0, c->stream>>>(c->g, c->u0, scale_dev);
-    c->launches++;
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? TL_OK : cuda_fail(e, "absmax launch");
+// max|u0| and max|r0| into w->scale
+int scales(Chunk *c, Warm *w) {
+    TL_CUDA(cudaMemsetAsync(w->scale, 0, 2 * sizeof(float), c->stream));
+    k_absmax2<<<kGramBlocks, 256, 0, c->stream>>>(c->g, c->u0, w->r0, w->scale);
+    return launched(c, "absmax launch");
 }
 
-// u = u0 + network(features): call after common_init (u0, Kx, Ky current)
-int warm_apply(Chunk *c) {
-    Warm *w = warm_of(c);
-    if (!w) {
-        set_error("warm start requested but no model is loaded (tl_set_warm_start_model)");
-        return TL_ERR_STATE;
-    }
+// dnet = network(features) (call after common_init, with r0 and dprev current)
+int net_direction(Chunk *c, Warm *w) {
     cudaStream_t s = c->stream;
     int rc;
-    if ((rc = warm_scale(c, w->scale))) return rc;
-    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, c->density, c->kx, c->ky, w->scale, c->dt, w->x,
-                                    w->nxp, nullptr);
-    c->launches++;
+    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->dprev, c->density, c->kx, c->ky, w->scale,
+                                    c->dt, w->x, w->nxp, nullptr);
+    if ((rc = launched(c, "features launch"))) return rc;
     bf16 *h = w->h0, *hn = w->h1;
     if ((rc = tl_nn_conv(0, 16, 32, w->x, w->wf[0], w->bias[0], nullptr, h, w->pre, nullptr, 1, c->ny,
                          w->nxp, s)))
@@ -208,51 +322,178 @@ int warm_apply(Chunk *c) {
                          w->nxp, s)))
         return rc;
     c->launches += 6;
-    k_apply<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->y, w->nxp, w->scale);
-    c->launches++;
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? TL_OK : cuda_fail(e, "warm start apply");
+    k_dnet<<<1216, 256, 0, s>>>(c->g, w->y, w->nxp, w->scale, w->dnet);
+    return launched(c, "network direction");
 }
 
-int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *rr) {
+// coefficients (a, b) minimising phi over u0 + a dn + b dp; returns the
+// energy decrease times two (a bn + b bp), 0 when no direction helps
+double galerkin(const double *S, bool use_n, bool use_p, double *a, double *b) {
+    const double gnn = S[0], gnp = S[1], gpp = S[2], bn = S[3], bp = S[4];
+    *a = 0.0;
+    *b = 0.0;
+    const bool ok_n = use_n && gnn > 0.0 && isfinite(gnn) && isfinite(bn);
+    const bool ok_p = use_p && gpp > 0.0 && isfinite(gpp) && isfinite(bp);
+    double best = 0.0;
+    if (ok_n && ok_p) {
+        const double det = gnn * gpp - gnp * gnp;
+        if (isfinite(det) && det > 1e-12 * gnn * gpp) {
+            const double x = (bn * gpp - bp * gnp) / det, y = (gnn * bp - gnp * bn) / det;
+            const double gain = x * bn + y * bp;
+            if (isfinite(gain) && gain > 0.0) {
+                *a = x;
+                *b = y;
+                return gain;
+            }
+        }
+    }
+    if (ok_n && bn * bn / gnn > best) {
+        best = bn * bn / gnn;
+        *a = bn / gnn;
+        *b = 0.0;
+    }
+    if (ok_p && bp * bp / gpp > best) {
+        best = bp * bp / gpp;
+        *a = 0.0;
+        *b = bp / gpp;
+    }
+    return best;
+}
+
+}  // namespace
+
+void warm_free(Chunk *c) {
+    Warm *w = warm_of(c);
+    if (!w) return;
+    free_model(w);
+    for (void *p : w->allocs) cudaFree(p);
+    delete w;
+    c->warm = nullptr;
+}
+
+void warm_reset(Chunk *c) {
+    if (Warm *w = warm_of(c)) w->have_prev = false;
+}
+
+long long warm_param_count() {
+    long long n = 0;
+    for (int l = 0; l < kLayers; ++l) n += layer_floats(l);
+    return n;
+}
+
+int warm_set_model(Chunk *c, const float *params, long long n) {
+    if (n != warm_param_count()) {
+        set_error("warm start model: %lld parameters, expected %lld", n, warm_param_count());
+        return TL_ERR_ARG;
+    }
+    Warm *w;
     int rc;
-    // the plain start u = u^n: its residual defines the exit test
+    if ((rc = warm_state(c, &w))) return rc;
+    free_model(w);
+    cudaStream_t s = c->stream;
+    void *p;
+    auto &L = w->model_allocs;
+    if ((rc = dmalloc(L, &p, sizeof(float) * n, s))) return rc;
+    w->params = (float *)p;
+    TL_CUDA(cudaMemcpyAsync(w->params, params, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    long long off = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        if ((rc = dmalloc(L, &p, sizeof(bf16) * 9 * kCin[l] * kCout[l], s))) return rc;
+        w->wf[l] = (bf16 *)p;
+        if ((rc = tl_nn_pack(w->params + off, w->wf[l], nullptr, kCin[l], kCout[l], s))) return rc;
+        w->bias[l] = w->params + off + 9LL * kCin[l] * kCout[l];
+        off += layer_floats(l);
+    }
+    w->nxp = (c->nx + 15) / 16 * 16;
+    const size_t px = (size_t)(c->ny + 2) * (w->nxp + 2);
+    if ((rc = dmalloc(L, &p, sizeof(bf16) * px * 16, s))) return rc;
+    w->x = (bf16 *)p;
+    bf16 **acts[3] = {&w->h0, &w->h1, &w->pre};
+    for (bf16 **a : acts) {
+        if ((rc = dmalloc(L, &p, sizeof(bf16) * px * 32, s))) return rc;
+        *a = (bf16 *)p;
+    }
+    if ((rc = dmalloc(L, &p, sizeof(float) * (size_t)c->ny * w->nxp, s))) return rc;
+    w->y = (float *)p;
+    TL_CUDA(cudaStreamSynchronize(s));
+    w->model = true;
+    return TL_OK;
+}
+
+bool warm_ready(Chunk *c) { return warm_of(c) != nullptr && warm_of(c)->model; }
+
+int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *rr) {
+    const bool learned = c->cfg.warm_start == TL_WARM_LEARNED;
+    Warm *w;
+    int rc;
+    if ((rc = warm_state(c, &w))) return rc;
+    if (learned && !w->model) {
+        set_error("warm start requested but no model is loaded (tl_set_warm_start_model)");
+        return TL_ERR_STATE;
+    }
+    info->warm_used = 0;
+    info->warm_ratio = 1.0;
+    cudaStream_t s = c->stream;
+    // the plain start u = u^n: r = u^n - A u^n, its norm defines the exit test
     if ((rc = launch_residual(c, kEpiStore))) return rc;
+    if ((rc = launch_copy(c, w->r0, c->r, false))) return rc;
+    const bool have_prev = w->have_prev;
+    k_prev<<<1216, 256, 0, s>>>(c->g, c->u0, w->uprev, w->dprev, have_prev ? 1 : 0);
+    if ((rc = launched(c, "previous step launch"))) return rc;
+    w->have_prev = true;
+    if (learned) {
+        if ((rc = scales(c, w))) return rc;
+        if ((rc = net_direction(c, w))) return rc;
+    }
+    const double *dn = learned ? w->dnet : nullptr;
+    const double *dp = have_prev ? w->dprev : nullptr;
+    double S[kGramSums] = {0, 0, 0, 0, 0, 0};
+    if (dn || dp) {
+        k_gram<<<kGramBlocks, 256, 0, s>>>(c->g, dn, dp, w->r0, c->diag, c->kx, c->ky, w->partials);
+        if ((rc = launched(c, "gram launch"))) return rc;
+        std::vector<double> part((size_t)kGramBlocks * kGramSums);
+        TL_CUDA(cudaMemcpyAsync(part.data(), w->partials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
+                                s));
+        TL_CUDA(cudaStreamSynchronize(s));
+        for (int b = 0; b < kGramBlocks; ++b)
+            for (int q = 0; q < kGramSums; ++q) S[q] += part[(size_t)b * kGramSums + q];
+    }
     if ((rc = chunk_sync_scalars(c))) return rc;
     const double rr0 = c->sc_host->sum[0];
     *r0 = sqrt(fabs(rr0));
     *rr = rr0;
-    info->warm_used = 0;
-    info->warm_ratio = 1.0;
-    if ((rc = warm_apply(c))) return rc;
+    double a = 0.0, b = 0.0;
+    const double gain = galerkin(S, dn != nullptr, dp != nullptr, &a, &b);
+    if (!(gain > 0.0)) return TL_OK;  // the plain start: u = u^n, r = r0
+    k_combine<<<1216, 256, 0, s>>>(c->g, c->u0, a != 0.0 ? dn : nullptr, a, b != 0.0 ? dp : nullptr, b, c->u);
+    if ((rc = launched(c, "warm start combine"))) return rc;
     if ((rc = launch_residual(c, kEpiStore))) return rc;
     if ((rc = chunk_sync_scalars(c))) return rc;
     const double rrw = c->sc_host->sum[0];
+    info->warm_used = 1;
     info->warm_ratio = sqrt(fabs(rrw)) / (*r0 > 0.0 ? *r0 : 1.0);
-    if (isfinite(rrw) && rrw < rr0) {
-        info->warm_used = 1;
-        *rr = rrw;
-        return TL_OK;
-    }
-    // fallback to the plain start
-    if ((rc = launch_copy(c, c->u, c->u0, false))) return rc;
-    return launch_residual(c, kEpiNone);
+    *rr = rrw;
+    return TL_OK;
 }
 
-// FP32 [ny][nx][6] features + target of the solved step into dst (device)
+// FP32 [ny][nx][8] network inputs + target of the solved step into dst
+// (device); needs the previous-step tracking of a warm-started solve
 int warm_features(Chunk *c, float *dst) {
-    float *scale = nullptr;
-    TL_CUDA(cudaMallocAsync((void **)&scale, 256, c->stream));
-    int rc = warm_scale(c, scale);
-    if (rc == TL_OK) {
-        k_features<<<1216, 256, 0, c->stream>>>(c->g, c->u0, c->u, c->density, c->kx, c->ky, scale, c->dt,
-                                                nullptr, 0, dst);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) rc = cuda_fail(e, "features launch");
+    Warm *w = warm_of(c);
+    if (!w || !w->have_prev) {
+        set_error("tl_warm_start_features: solve the step with tl_warm_start prev or learned first");
+        return TL_ERR_STATE;
     }
-    cudaFreeAsync(scale, c->stream);
-    TL_CUDA(cudaStreamSynchronize(c->stream));
-    return rc;
+    cudaStream_t s = c->stream;
+    int rc;
+    k_resid0<<<1216, 256, 0, s>>>(c->g, c->u0, c->diag, c->kx, c->ky, w->r0);
+    if ((rc = launched(c, "residual launch"))) return rc;
+    if ((rc = scales(c, w))) return rc;
+    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->dprev, c->density, c->kx, c->ky, w->scale,
+                                    c->dt, nullptr, 0, dst);
+    if ((rc = launched(c, "features launch"))) return rc;
+    TL_CUDA(cudaStreamSynchronize(s));
+    return TL_OK;
 }
 
 }  // namespace tl

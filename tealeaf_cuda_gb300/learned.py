@@ -1,14 +1,16 @@
-"""Learned warm start: seeded random decks, trajectory data from the plain
-solver, the trainer of the residual network on the project's own BF16
-tensor-core kernels (tl_nn_* in csrc/tl_conv.cu), model files, and the
-evaluation of what the network saves over the plain start.
+"""Learned warm start: seeded random decks, trajectory data from the solver,
+the trainer of the residual network on the project's own BF16 tensor-core
+kernels (tl_nn_* in csrc/tl_conv.cu), model files, and the evaluation of
+what the warm starts save over the plain start.
 
-Network (tl_warm.cu): inputs (u^n / s, log density, log1p Kx, log1p Ky,
-100 dt) with s = max|u^n|, six 3x3 convolutions of 32 channels (GELU, four
-residual blocks), output du / s; the solve starts from u^n + du when that
-lowers the residual and keeps tl_eps * (plain start residual) as its test.
-Torch only allocates device buffers here; every FLOP of the network runs in
-the library's kernels.
+Network (tl_warm.cu): inputs (u^n / max|u^n|, log density, log1p Kx,
+log1p Ky, 100 dt, r0 / max|r0|, d_prev / max|r0|) with r0 = u^n - A u^n and
+d_prev = u^n - u^{n-1}; six 3x3 convolutions of 32 channels (GELU, four
+residual blocks); output (u^{n+1} - u^n) / max|r0|.  The solve starts from
+u^n + a d_net + b d_prev with the energy-minimising (a, b) and keeps
+tl_eps * (plain start residual) as its exit test.  Torch only allocates
+device buffers here; every FLOP of the network runs in the library's
+kernels.
 """
 import ctypes as C
 import math
@@ -19,6 +21,8 @@ import numpy as np
 from . import Chunk, load, parse_deck
 
 LAYERS = [(16, 32, 0)] + [(32, 32, 1)] * 4 + [(32, 16, 2)]  # (cin, coutp, conv mode)
+NFEAT = 8           # per cell: seven network inputs + the target
+WARM = {"none": 0, "learned": 1, "prev": 2}  # TL_WARM_*
 MASK64 = (1 << 64) - 1
 
 
@@ -125,15 +129,17 @@ def load_model(path):
 # ----------------------------------------------------------------- data
 
 def trajectories(seeds, n, steps, device="cuda:0", precond="jac_diag"):
-    """Solve `steps` timesteps of each seeded deck with the plain FP64 solver
-    and keep, per step, [n][n][6] = (features of u^n, (u^{n+1} - u^n) / s)."""
+    """Solve `steps` timesteps of each seeded deck (FP64, previous-step warm
+    start, which tracks u^{n-1}) and keep, per step, [n][n][NFEAT] = (network
+    inputs of step n, (u^{n+1} - u^n) / max|r0|)."""
     import torch
     lib = load()
-    data = torch.empty((len(seeds) * steps, n, n, 6), dtype=torch.float32, device=device)
+    data = torch.empty((len(seeds) * steps, n, n, NFEAT), dtype=torch.float32, device=device)
     iters = []
     k = 0
     for seed in seeds:
         cfg = parse_deck(random_deck(seed, n, steps, precond=precond))
+        cfg.warm_start = WARM["prev"]
         with Chunk(cfg) as ch:
             ch.start()
             for _ in range(steps):
@@ -151,18 +157,19 @@ def trajectory_crops(seeds, n, steps, crops_per_step, crop=144, seed=0, device="
     """Like trajectories(), but keeps `crops_per_step` random crop x crop
     windows of every `every`-th step instead of whole fields (a 3x3-conv
     network is translation-equivariant, so crops are enough to train it and
-    keep large grids in memory).  Returns ([N][crop][crop][6], iterations)."""
+    keep large grids in memory).  Returns ([N][crop][crop][NFEAT], iterations)."""
     import torch
     lib = load()
     rng = np.random.default_rng(seed)
     kept = sum(1 for s in range(steps) if s % every == 0)
-    data = torch.empty((len(seeds) * kept * crops_per_step, crop, crop, 6), dtype=torch.float32,
+    data = torch.empty((len(seeds) * kept * crops_per_step, crop, crop, NFEAT), dtype=torch.float32,
                        device=device)
-    full = torch.empty((n, n, 6), dtype=torch.float32, device=device)
+    full = torch.empty((n, n, NFEAT), dtype=torch.float32, device=device)
     iters = []
     k = 0
     for sd in seeds:
         cfg = parse_deck(random_deck(sd, n, steps, precond=precond))
+        cfg.warm_start = WARM["prev"]
         with Chunk(cfg) as ch:
             ch.start()
             for s in range(steps):
@@ -283,7 +290,7 @@ class Trainer:
                                 self.S, self.margin, self.stream), "loss")
 
     def step(self, data, rng):
-        """one Adam step on a batch of random crops of `data` ([N][H][W][6])"""
+        """one Adam step on a batch of random crops of `data` ([N][H][W][NFEAT])"""
         torch = self.torch
         N, H, W, F = data.shape
         S = self.S
@@ -324,15 +331,18 @@ def train(data, iters=1500, batch=16, crop=144, lr=2e-3, seed=0, init=None, log_
 
 # ------------------------------------------------------------ evaluation
 
-def solve_with(params, deck, steps):
-    """Per-step solve info of a deck, with the model (params) or the plain start (None)."""
+def solve_with(mode, params, deck, steps, precision=None):
+    """Per-step solve info of a deck with warm start `mode` ("none", "prev"
+    or "learned"; params = the model of "learned")."""
     lib = load()
     cfg = parse_deck(deck)
-    cfg.warm_start = 1 if params is not None else 0
+    cfg.warm_start = WARM[mode]
+    if precision is not None:
+        cfg.precision = precision
     out = []
     with Chunk(cfg) as ch:
         ch.start()
-        if params is not None:
+        if mode == "learned":
             p = np.ascontiguousarray(params, dtype=np.float32)
             assert lib.tl_set_warm_start_model(ch._h, C.c_void_p(p.ctypes.data), p.size) == 0
         for _ in range(steps):
@@ -343,22 +353,32 @@ def solve_with(params, deck, steps):
 
 
 def evaluate(params, seeds, n, steps, precond="jac_diag"):
-    """Compare the learned start with the plain one on held-out decks."""
+    """Iterations of the plain, previous-step and learned starts on held-out decks."""
     rows = []
     for seed in seeds:
         deck = random_deck(seed, n, steps, precond=precond)
-        plain = solve_with(None, deck, steps)
-        warm = solve_with(params, deck, steps)
-        rows.append({"seed": seed,
-                     "plain_iters": [r["iterations"] for r in plain],
-                     "warm_iters": [r["iterations"] for r in warm],
-                     "warm_used": [r["warm_used"] for r in warm],
-                     "warm_ratio": [r["warm_ratio"] for r in warm],
-                     "plain_seconds": sum(r["seconds"] for r in plain),
-                     "warm_seconds": sum(r["seconds"] for r in warm),
-                     "summary_rel_diff": max(abs(a - b) / abs(a) for a, b in
-                                             zip(plain[-1]["summary"], warm[-1]["summary"]))})
+        runs = {m: solve_with(m, params, deck, steps) for m in ("none", "prev", "learned")}
+        plain = runs["none"]
+        row = {"seed": seed}
+        for m, r in runs.items():
+            row[m + "_iters"] = [x["iterations"] for x in r]
+            row[m + "_seconds"] = sum(x["seconds"] for x in r)
+            row[m + "_ratio"] = [x["warm_ratio"] for x in r]
+            row[m + "_summary_rel_diff"] = max(abs(a - b) / abs(a) for a, b in
+                                               zip(plain[-1]["summary"], r[-1]["summary"]))
+        rows.append(row)
     return rows
+
+
+def summarise(rows):
+    """totals of evaluate()'s rows"""
+    out = {}
+    for m in ("none", "prev", "learned"):
+        out[m + "_iterations"] = sum(sum(r[m + "_iters"]) for r in rows)
+        out[m + "_seconds"] = sum(r[m + "_seconds"] for r in rows)
+        out[m + "_max_summary_rel_diff"] = max(r[m + "_summary_rel_diff"] for r in rows)
+    out["solves"] = sum(len(r["none_iters"]) for r in rows)
+    return out
 
 
 def main(argv=None):
@@ -407,15 +427,7 @@ def main(argv=None):
     else:
         lo, hi = (int(x) for x in a.seeds.split("-"))
         rows = evaluate(load_model(a.model), list(range(lo, hi + 1)), a.n, a.steps)
-        plain = sum(sum(r["plain_iters"]) for r in rows)
-        warm = sum(sum(r["warm_iters"]) for r in rows)
-        rep = {"n": a.n, "steps": a.steps, "seeds": a.seeds, "plain_iterations": plain,
-               "learned_iterations": warm, "iteration_ratio": warm / max(plain, 1),
-               "plain_seconds": sum(r["plain_seconds"] for r in rows),
-               "learned_seconds": sum(r["warm_seconds"] for r in rows),
-               "learned_start_kept": sum(sum(r["warm_used"]) for r in rows),
-               "solves": sum(len(r["warm_used"]) for r in rows),
-               "max_summary_rel_diff": max(r["summary_rel_diff"] for r in rows), "decks": rows}
+        rep = {"n": a.n, "steps": a.steps, "seeds": a.seeds, **summarise(rows), "decks": rows}
         print(json.dumps({k: v for k, v in rep.items() if k != "decks"}))
         if a.report:
             json.dump(rep, open(a.report, "w"), indent=1)

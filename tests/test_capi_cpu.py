@@ -80,6 +80,12 @@ def test_deck_parser_defaults_and_flags():
     assert cfg.reflective_boundary == 1 and cfg.check_result == 1 and cfg.coefficient == 2
     assert cfg.precision == tl.PRECISION_MIXED and cfg.inner_eps == 1e-5
     assert cfg.eps == 1e-10 and cfg.end_step == 640000 and cfg.summary_frequency == 10
+    assert cfg.warm_start == tl.WARM_NONE
+    for word, mode in (("none", tl.WARM_NONE), ("prev", tl.WARM_PREV), ("learned", tl.WARM_LEARNED)):
+        cfg = tl.parse_deck(text.replace("halo_depth=2", f"tl_warm_start {word}"))
+        assert cfg.warm_start == mode
+    with pytest.raises(ValueError, match="tl_warm_start"):
+        tl.parse_deck(text.replace("halo_depth=2", "tl_warm_start guess"))
 
 
 @pytest.mark.parametrize("bad,msg", [("*tea\nx_cells 10\n*endtea\n", "No states"),
