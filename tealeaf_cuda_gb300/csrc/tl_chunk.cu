@@ -118,6 +118,8 @@ static int chunk_alloc(const tl_config_t *cfg, Chunk **out) {
     c->g.tiles = c->g.tiles_x * c->g.tiles_y;
     c->first = true;
     c->dt = cfg->dtinit;
+    c->inner_fuse = kInnerFuseDefault;
+    c->inner_seg = kInnerSegDefault;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     c->grid_red = sms > 0 ? sms * 4 : 512;
@@ -264,12 +266,7 @@ int chunk_upload_coefs(Chunk *c, const double *a, const double *b, int n) {
         c->ch_alphas = na;
         c->ch_betas = nb;
         c->n_coefs_cap = n;
-        // graphs captured the old pointers
-        for (cudaGraphExec_t &g : c->graphs)
-            if (g) {
-                cudaGraphExecDestroy(g);
-                g = nullptr;
-            }
+        drop_graphs(c);  // graphs captured the old pointers
     }
     if (n == 0) return TL_OK;
     TL_CUDA(cudaMemcpyAsync(c->ch_alphas, a, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -333,6 +330,14 @@ static int field_summary(Chunk *c, double *vol, double *mass, double *ie, double
     if (ie) *ie = c->sc_host->sum[2];
     if (temp) *temp = c->sc_host->sum[3];
     return TL_OK;
+}
+
+void drop_graphs(Chunk *c) {
+    for (cudaGraphExec_t &g : c->graphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
 }
 
 }  // namespace tl
@@ -510,6 +515,22 @@ int tl_warm_start_features(tl_chunk_t *ch, float *dst) {
         return TL_ERR_ARG;
     }
     return warm_features(ch->c, dst);
+}
+
+int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips) {
+    if (!ch || !ch->c) {
+        set_error("tl_set_inner_fusion: no chunk");
+        return TL_ERR_STATE;
+    }
+    if (steps < 1 || steps > 4 || seg_strips < 1) {
+        set_error("tl_set_inner_fusion: steps must be 1..4 and seg_strips >= 1 (got %d, %d)", steps, seg_strips);
+        return TL_ERR_ARG;
+    }
+    Chunk *c = ch->c;
+    if (c->inner_fuse != steps || c->inner_seg != seg_strips) drop_graphs(c);
+    c->inner_fuse = steps;
+    c->inner_seg = seg_strips;
+    return TL_OK;
 }
 
 int tl_set_profiling(tl_chunk_t *ch, int on) {

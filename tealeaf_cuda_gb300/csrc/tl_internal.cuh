@@ -124,6 +124,8 @@ struct Chunk {
     int grid_red;                // CTAs of the grid-stride kernels
     // mixed precision state (allocated on first use)
     void *mixed;
+    int inner_fuse;              // FP32 PPCG inner steps per HBM pass (1: one kernel per step)
+    int inner_seg;               // 4-row strips per CTA segment of the fused inner kernel
     // learned warm start model and buffers (tl_warm.cu)
     void *warm;
     double rx, ry;
@@ -212,6 +214,9 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
 int mixed_ppcg_prepare(Chunk *c);  // FP32 operator + preconditioner copies
 int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
+void drop_graphs(Chunk *c);        // after a change that captured graphs depend on
+constexpr int kInnerFuseDefault = 4;
+constexpr int kInnerSegDefault = 32;
 // warm starts (tl_warm.cu)
 void warm_free(Chunk *c);
 void warm_reset(Chunk *c);                // forget u^(n-1) (tl_start)

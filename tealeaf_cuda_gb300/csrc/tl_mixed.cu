@@ -33,6 +33,7 @@ namespace {
 struct Mixed {
     float *kx, *ky, *mi, *d, *r, *p, *w, *z;
     float *sd[2], *rtemp, *utemp, *cp, *bfp;   // PPCG inner steps
+    float *rtemp2;                             // second rtemp of the fused inner passes
     double *partials;            // one per CTA of the vectorised kernels
     unsigned int *counter;
     int vtiles_x, vtiles;        // tiles of the vectorised kernels
@@ -542,6 +543,178 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
     }
 }
 
+// ---------------------------- temporally blocked PPCG inner steps (FP32)
+//
+// T inner steps per pass over HBM (the matrix-powers idea of the
+// reference's halo_depth > 1 PPCG, tea_leaf_ppcg.f90:199-221, done inside one
+// chunk).  A CTA owns a band of kFusedThreads columns (one column per
+// thread, T columns of halo on each side, recomputed) and a segment of
+// `seg` 4-row strips, and streams down the strips as a pipeline: at
+// iteration s, level 0 loads strip s (sd, rtemp, utemp) and level t = 1..T
+// applies inner step t to strip s - t, from level t-1's strips s-t-1 (last
+// row), s-t and s-t+1 (first row).  Vertical neighbours stay in the
+// thread's registers, horizontal ones go through shared memory (a buffer
+// per level and iteration parity: one barrier per strip).  Level T stores
+// its strip when it lies in the CTA's band and segment.  sd and rtemp are
+// read in halos that other CTAs own, so they ping-pong between launches;
+// utemp is read and written only at owned cells (its halo values are never
+// stored) and is updated in place.  Every value is computed with the
+// operations of k_pp_step in the same order, so T fused steps give the
+// bits of T single steps.
+constexpr int kFusedThreads = 256;
+constexpr int kFusedMax = 4;       // most steps fused into one pass
+
+struct PpFusedArgs {
+    int nx, ny, h, pitch, pitch64, seg, band;
+    const float *sd_in, *rt_in;
+    float *sd_out, *rt_out, *utemp;
+    const float *kx, *ky, *mi, *cp, *bfp;
+    const double *alphas, *betas;
+    int step0;                      // inner step of level 1 (1-based)
+    double *z64;                    // LAST: z = utemp in FP64
+};
+
+template <int T, int PC, bool LAST>
+__global__ void __launch_bounds__(kFusedThreads) k_pp_fused(PpFusedArgs a, const DevScalars *__restrict__ sc) {
+    if (*(volatile const int *)&sc->done) return;
+    __shared__ float xs[T][2][4][kFusedThreads];
+    const int tid = threadIdx.x;
+    const int col = blockIdx.x * a.band - T + tid;
+    const bool incol = col >= 0 && col < a.nx;
+    const bool own = incol && tid >= T && tid < T + a.band;
+    const int nstrips = (a.ny + 3) >> 2;
+    const int sb = blockIdx.y * a.seg;
+    const int se = min(sb + a.seg, nstrips);
+    const int64_t P = a.pitch;
+    float al[T], be[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+        al[t] = (float)a.alphas[a.step0 + t - 1];
+        be[t] = (float)a.betas[a.step0 + t - 1];
+    }
+#pragma unroll
+    for (int l = 0; l < T; ++l)
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) xs[l][p][k][tid] = 0.f;
+    // per producer level l < T: its output strip of the previous iteration
+    // (sd, rtemp, utemp) and the last sd row of the one before
+    float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
+#pragma unroll
+    for (int l = 0; l < T; ++l) {
+        sdL[l] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) sdP[l][k] = rtP[l][k] = utP[l][k] = 0.f;
+    }
+    // level 0 loads, one strip ahead
+    float ldS[4], ldR[4], ldU[4];
+    auto load = [&](int s) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int row = 4 * s + k;
+            const bool v = incol && s >= 0 && row < a.ny;
+            const int64_t i = (int64_t)(col + a.h) + (int64_t)(row + a.h) * P;
+            ldS[k] = v ? a.sd_in[i] : 0.f;
+            ldR[k] = v ? a.rt_in[i] : 0.f;
+            ldU[k] = v ? a.utemp[i] : 0.f;
+        }
+    };
+    load(sb - T);
+    __syncthreads();
+    for (int s = sb - T; s < se + T; ++s) {
+        float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            cS[k] = ldS[k];
+            cR[k] = ldR[k];
+            cU[k] = ldU[k];
+            xs[0][s & 1][k][tid] = ldS[k];
+        }
+        if (s + 1 < se + T) load(s + 1);
+#pragma unroll
+        for (int t = 1; t <= T; ++t) {
+            const int q = s - t;
+            const int m = (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
+            const int64_t i0 = (int64_t)(col + a.h) + (int64_t)(4 * q + a.h) * P;
+            const float(&x0)[4] = sdP[t - 1];
+            const int pr = (s - 1) & 1;
+            float oS[4], oR[4], oU[4], z[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                oS[k] = oR[k] = oU[k] = z[k] = 0.f;
+                if (k < m) {
+                    const int64_t i = i0 + (int64_t)k * P;
+                    const float c = x0[k];
+                    const float n = k < 3 ? x0[k + 1] : cS[0];
+                    const float sv = k > 0 ? x0[k - 1] : sdL[t - 1];
+                    const float w = tid > 0 ? xs[t - 1][pr][k][tid - 1] : 0.f;
+                    const float e = tid < kFusedThreads - 1 ? xs[t - 1][pr][k][tid + 1] : 0.f;
+                    oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, w, e, __ldg(&a.ky[i + P]), __ldg(&a.ky[i]),
+                                                       __ldg(&a.kx[i + 1]), __ldg(&a.kx[i]));
+                }
+            }
+            if constexpr (PC == TL_PREC_JAC_BLOCK) {
+                // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
+                // z_k = dp_k - cp_k z_{k+1}
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (k < m) {
+                        const int64_t i = i0 + (int64_t)k * P;
+                        const float bf = __ldg(&a.bfp[i]);
+                        z[k] = k == 0 ? oR[0] * bf : fmaf(__ldg(&a.ky[i]), z[k - 1], oR[k]) * bf;
+                    }
+                }
+#pragma unroll
+                for (int k = 2; k >= 0; --k)
+                    if (k < m - 1) z[k] = fmaf(-__ldg(&a.cp[i0 + (int64_t)k * P]), z[k + 1], z[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k < m)
+                        z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * __ldg(&a.mi[i0 + (int64_t)k * P]) : oR[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k < m) {
+                    oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
+                    oU[k] = utP[t - 1][k] + oS[k];
+                }
+            }
+            // level t-1 has been consumed: its output of this iteration moves in
+            sdL[t - 1] = sdP[t - 1][3];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                sdP[t - 1][k] = cS[k];
+                rtP[t - 1][k] = cR[k];
+                utP[t - 1][k] = cU[k];
+                cS[k] = oS[k];
+                cR[k] = oR[k];
+                cU[k] = oU[k];
+            }
+            if (t < T) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) xs[t][s & 1][k][tid] = oS[k];
+            } else if (own && q >= sb && q < se) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (k < m) {
+                        const int64_t i = i0 + (int64_t)k * P;
+                        if (LAST) {
+                            a.z64[(int64_t)(col + a.h) + (int64_t)(4 * q + k + a.h) * a.pitch64] = (double)oU[k];
+                        } else {
+                            a.sd_out[i] = oS[k];
+                            a.rt_out[i] = oR[k];
+                            a.utemp[i] = oU[k];
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // FP32 copies of the preconditioner: Mi = 1/diag, block cp, and bfp with
 // 1/diag at each strip's first row
 __global__ void k_pp_convert(GeoV g, int pitch64, const double *__restrict__ dg, const double *__restrict__ cp64,
@@ -627,7 +800,8 @@ int mixed_alloc(Chunk *c) {
     c->mixed = mx;
     const size_t n = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows + 32;
     float **arr[] = {&mx->kx, &mx->ky, &mx->mi,    &mx->d,     &mx->r,  &mx->p,  &mx->w,
-                     &mx->z,  &mx->sd[0], &mx->sd[1], &mx->rtemp, &mx->utemp, &mx->cp, &mx->bfp};
+                     &mx->z,  &mx->sd[0], &mx->sd[1], &mx->rtemp, &mx->utemp, &mx->cp, &mx->bfp,
+                     &mx->rtemp2};
     for (float **a : arr) {
         void *p = nullptr;
         cudaError_t e = cudaMalloc(&p, n * sizeof(float));
@@ -717,7 +891,23 @@ int mixed_ppcg_prepare(Chunk *c) {
     });
 }
 
-// the inner steps of tea_leaf_ppcg.f90:174-230 in FP32; z (FP64) at the end
+template <int T, int PC>
+void launch_fused(dim3 grid, cudaStream_t s, const PpFusedArgs &a, bool last, const DevScalars *sc) {
+    if (last) k_pp_fused<T, PC, true><<<grid, kFusedThreads, 0, s>>>(a, sc);
+    else k_pp_fused<T, PC, false><<<grid, kFusedThreads, 0, s>>>(a, sc);
+}
+
+template <int T>
+void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bool last, const DevScalars *sc) {
+    if (pc == TL_PREC_JAC_BLOCK) launch_fused<T, TL_PREC_JAC_BLOCK>(grid, s, a, last, sc);
+    else if (pc == TL_PREC_JAC_DIAG) launch_fused<T, TL_PREC_JAC_DIAG>(grid, s, a, last, sc);
+    else launch_fused<T, TL_PREC_NONE>(grid, s, a, last, sc);
+}
+
+// the inner steps of tea_leaf_ppcg.f90:174-230 in FP32; z (FP64) at the end.
+// With c->inner_fuse > 1 the steps run as ceil(inner / inner_fuse) passes of
+// k_pp_fused (sizes as even as possible, larger first); otherwise one
+// k_pp_step per step.
 int mixed_ppcg_inner(Chunk *c) {
     Mixed *mx = mixed_of(c);
     const int inner = c->cfg.ppcg_inner_steps;
@@ -739,6 +929,52 @@ int mixed_ppcg_inner(Chunk *c) {
                                                                 mx->utemp, c->sc);
          })))
         return rc;
+    const int fuse = c->inner_fuse < 1 ? 1 : (c->inner_fuse > kFusedMax ? kFusedMax : c->inner_fuse);
+    if (fuse > 1) {
+        float *rt[2] = {mx->rtemp, mx->rtemp2};
+        const int passes = (inner + fuse - 1) / fuse;
+        const int nstrips = (c->ny + 3) / 4;
+        int done = 0;
+        for (int l = 0; l < passes; ++l) {
+            const int T = (inner - done + (passes - l) - 1) / (passes - l);
+            const bool last = l == passes - 1;
+            PpFusedArgs a;
+            a.nx = c->nx;
+            a.ny = c->ny;
+            a.h = c->h;
+            a.pitch = c->pitch;
+            a.pitch64 = c->pitch;
+            a.seg = c->inner_seg;
+            if ((nstrips + a.seg - 1) / a.seg > 65535) a.seg = (nstrips + 65534) / 65535;
+            a.band = kFusedThreads - 2 * T;
+            a.sd_in = mx->sd[l & 1];
+            a.sd_out = mx->sd[(l + 1) & 1];
+            a.rt_in = rt[l & 1];
+            a.rt_out = rt[(l + 1) & 1];
+            a.utemp = mx->utemp;
+            a.kx = mx->kx;
+            a.ky = mx->ky;
+            a.mi = mx->mi;
+            a.cp = mx->cp;
+            a.bfp = mx->bfp;
+            a.alphas = c->ch_alphas;
+            a.betas = c->ch_betas;
+            a.step0 = done + 1;
+            a.z64 = c->z;
+            const dim3 fg((unsigned)((c->nx + a.band - 1) / a.band), (unsigned)((nstrips + a.seg - 1) / a.seg));
+            rc = launch_v(c, "mixed_pp_fused", [&] {
+                switch (T) {
+                case 1: launch_fused_pc<1>(fg, s, a, pc, last, c->sc); break;
+                case 2: launch_fused_pc<2>(fg, s, a, pc, last, c->sc); break;
+                case 3: launch_fused_pc<3>(fg, s, a, pc, last, c->sc); break;
+                default: launch_fused_pc<4>(fg, s, a, pc, last, c->sc); break;
+                }
+            });
+            if (rc) return rc;
+            done += T;
+        }
+        return TL_OK;
+    }
     for (int st = 1; st <= inner; ++st) {
         const float *si = mx->sd[(st - 1) & 1];
         float *so = mx->sd[st & 1];

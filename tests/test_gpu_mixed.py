@@ -77,3 +77,34 @@ def test_mixed_ppcg_matches_fp64(precond):
         print(f"ppcg {precond} step {step}: outer its fp64 {i64['iterations']} mixed {imx['iterations']}, "
               f"max|du|/max|u| = {err:.2e}")
         assert err < 1e-9
+
+
+@pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
+def test_fused_inner_steps_are_bitwise_equal(precond):
+    """The temporally blocked inner steps (2-4 per pass, any segment height)
+    give the bits of one kernel per inner step; 600 x 150 cells make several
+    column bands, a partial last strip and many row segments."""
+    deck = decks.make_deck(x_cells=600, y_cells=150, end_step=2, tl_preconditioner_type=precond, tl_use_cg=False,
+                           tl_use_ppcg=True, tl_ppcg_inner_steps=10, tl_ch_cg_presteps=10,
+                           tl_ch_cg_epslim=1.0e10, tl_precision="mixed")
+    runs = {}
+    for steps, seg in [(1, 32), (2, 32), (3, 4), (4, 4), (4, 1), (2, 7)]:
+        cfg = tl.parse_deck(deck)
+        with tl.Chunk(cfg) as ch:
+            ch.set_inner_fusion(steps, seg)
+            ch.start()
+            its = [ch.timestep()["iterations"] for _ in range(2)]
+            runs[(steps, seg)] = (its, ch.interior("u").copy(), ch.field_summary())
+    its0, u0, fs0 = runs[(1, 32)]
+    for key, (its, u, fs) in runs.items():
+        assert its == its0, key
+        assert np.array_equal(u, u0), key
+        assert fs == fs0, key
+
+
+def test_inner_fusion_rejects_bad_settings():
+    cfg = tl.parse_deck(decks.make_deck(x_cells=32, y_cells=32, end_step=1))
+    with tl.Chunk(cfg) as ch:
+        for bad in [(0, 32), (5, 32), (2, 0)]:
+            with pytest.raises(tl.TeaLeafError):
+                ch.set_inner_fusion(*bad)
