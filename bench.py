@@ -81,6 +81,8 @@ BYTES_PER_CELL = {
     "finalise": 24,
     "ppcg_p": 24,        # read z, p; write p
     "copy": 16,          # read src; write dst
+    "ppcg_store_zr": 24,  # read r, z; write r_store
+    "ppcg_rrn": 24,      # read r, r_store, z
     # mixed precision: FP32 inner iteration (4-byte elements)
     "mixed_w": 16,       # read p, Kx, Ky; write w
     "mixed_ur": 32,      # jac_diag: read d, p, r, w, Mi; write d, r, z
@@ -98,6 +100,13 @@ def bytes_per_cell(kernel, precond):
         # read sd, Kx, Ky, rtemp, utemp + the preconditioner (Mi; or cp and
         # 1/b of the strip solve); write sd', rtemp, utemp (an inner step
         # before the last)
+        return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
+    if kernel == "mixed_pp_ur":
+        # read u, p, w, r (FP64) + the preconditioner (Mi; or diag, Ky, cp,
+        # bfp); write u, r (FP64) and rtemp, sd, utemp (FP32)
+        return {"none": 60, "jac_diag": 68, "jac_block": 92}[precond]
+    if kernel == "mixed_pp_fused":
+        # the same arrays once per pass of several inner steps
         return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
     return BYTES_PER_CELL.get(kernel)
 

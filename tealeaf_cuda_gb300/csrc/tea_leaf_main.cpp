@@ -1,6 +1,7 @@
 // tea_leaf_main.cpp -- the `tea_leaf` executable: reads a deck (./tea.in by
 // default), writes tea.out, echoes the log like the reference program.
-//   tea_leaf [deck] [--out FILE] [--legacy-abi] [--max-steps N] [--quiet]
+//   tea_leaf [deck] [--out FILE] [--legacy-abi] [--max-steps N] [--quiet] [--model FILE]
+// --model names the network of `tl_warm_start learned` (a TLWS0001 file).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -19,6 +20,7 @@ int main(int argc, char **argv) {
         else if (!strcmp(argv[i], "--legacy-abi")) o.legacy_abi = 1;
         else if (!strcmp(argv[i], "--max-steps") && i + 1 < argc) o.max_steps = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--quiet")) o.echo = 0;
+        else if (!strcmp(argv[i], "--model") && i + 1 < argc) o.model_path = argv[++i];
         else deck = argv[i];
     }
     FILE *f = fopen(deck, "rb");

@@ -184,6 +184,7 @@ int launch_ppcg_calc_sd_new(Chunk *c, int step, bool fast);
 int launch_copy(Chunk *c, double *dst, const double *src, bool fast);
 int launch_ppcg_rrn(Chunk *c, int epi, bool fast);
 int launch_ppcg_zr(Chunk *c, int epi, bool fast);
+int launch_ppcg_store_zr(Chunk *c, int epi, bool fast);  // r_store = r + ppcg_zr
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast);
 int launch_jacobi(Chunk *c, int epi, bool fast);
 int launch_finalise(Chunk *c);
@@ -214,9 +215,10 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
 int mixed_ppcg_prepare(Chunk *c);  // FP32 operator + preconditioner copies
 int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
+int mixed_ppcg_ur_inner(Chunk *c); // the outer u/r update fused with the inner start, then the steps
 void drop_graphs(Chunk *c);        // after a change that captured graphs depend on
 constexpr int kInnerFuseDefault = 4;
-constexpr int kInnerSegDefault = 32;
+constexpr int kInnerSegDefault = 64;
 // warm starts (tl_warm.cu)
 void warm_free(Chunk *c);
 void warm_reset(Chunk *c);                // forget u^(n-1) (tl_start)

@@ -21,6 +21,7 @@
 #include <stdio.h>
 
 #include "tl_internal.cuh"
+#include "tl_device.cuh"
 
 namespace tl {
 
@@ -228,32 +229,6 @@ __device__ __forceinline__ void strip_apply(const double *__restrict__ kx,
             const double b = fma(kxe, xe, kxc * xw);
             ax[k] = fma(diag, xr[k + 1], -a) - b;
             xc[k] = xr[k + 1];
-        }
-    }
-}
-
-// block-Jacobi strip solve z = M^-1 x (tea_block_jacobi.cuknl:11-46)
-__device__ __forceinline__ void strip_block_solve(const double *__restrict__ dg,
-                                                  const double *__restrict__ ky,
-                                                  const double *__restrict__ cp,
-                                                  const double *__restrict__ bfp, int pitch,
-                                                  int64_t base, int m, const double (&x)[4],
-                                                  double (&z)[4]) {
-    double dp[4];
-    dp[0] = x[0] / dg[base];
-#pragma unroll
-    for (int k = 1; k < 4; ++k)
-        if (k < m) {
-            const int64_t i = base + (int64_t)k * pitch;
-            dp[k] = fma(ky[i], dp[k - 1], x[k]) * bfp[i];
-        }
-#pragma unroll
-    for (int k = 3; k >= 0; --k) {
-        if (k == m - 1) {
-            z[k] = dp[k];
-        } else if (k < m - 1) {
-            const int64_t i = base + (int64_t)k * pitch;
-            z[k] = fma(-cp[i], z[k + 1], dp[k]);
         }
     }
 }
@@ -669,6 +644,24 @@ struct BodyCopy {
     }
 };
 
+struct BodyStoreZr {  // r_store = r and sum r.z in one pass (tea_leaf_ppcg.cuknl:302-313 + the
+                      // r.z norm); the sum is BodyNorm{r, z}'s, in the same order
+    const double *r, *z;
+    double *r_store;
+    int pitch;
+    __device__ void setup() {}
+    __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = base + (int64_t)k * pitch;
+                const double rv = r[i];
+                r_store[i] = rv;
+                acc[0] = fma(rv, z[i], acc[0]);
+            }
+    }
+};
+
 struct BodyPpcgRrn {  // sum (r - r_store).z  (tea_leaf_ppcg.cuknl:279-297)
     const double *r, *r_store, *z;
     int pitch;
@@ -1067,6 +1060,11 @@ int launch_ppcg_rrn(Chunk *c, int epi, bool fast) {
 int launch_ppcg_zr(Chunk *c, int epi, bool fast) {
     BodyNorm b{c->r, c->z, c->pitch};
     return run<1>(c, "ppcg_zr", b, epi, fast);
+}
+
+int launch_ppcg_store_zr(Chunk *c, int epi, bool fast) {
+    BodyStoreZr b{c->r, c->z, c->r_store, c->pitch};
+    return run<1>(c, "ppcg_store_zr", b, epi, fast);
 }
 
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast) {

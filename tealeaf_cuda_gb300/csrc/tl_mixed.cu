@@ -25,6 +25,7 @@
 #include <chrono>
 
 #include "tl_internal.cuh"
+#include "tl_device.cuh"
 
 namespace tl {
 
@@ -550,17 +551,20 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 // chunk).  A CTA owns a band of kFusedThreads columns (one column per
 // thread, T columns of halo on each side, recomputed) and a segment of
 // `seg` 4-row strips, and streams down the strips as a pipeline: at
-// iteration s, level 0 loads strip s (sd, rtemp, utemp) and level t = 1..T
+// iteration s, level 0 takes strip s (sd, rtemp, utemp and the strip's
+// coefficients, loaded from HBM during iteration s-1) and level t = 1..T
 // applies inner step t to strip s - t, from level t-1's strips s-t-1 (last
 // row), s-t and s-t+1 (first row).  Vertical neighbours stay in the
-// thread's registers, horizontal ones go through shared memory (a buffer
-// per level and iteration parity: one barrier per strip).  Level T stores
-// its strip when it lies in the CTA's band and segment.  sd and rtemp are
-// read in halos that other CTAs own, so they ping-pong between launches;
+// thread's registers; horizontal ones go through shared memory (a buffer
+// per level and iteration parity), and so do the coefficients (a ring of the
+// T+1 strips in flight), so a coefficient is read from HBM once per pass and
+// the levels never wait on global loads: one barrier per strip.  Level T
+// stores its strip when it lies in the CTA's band and segment.  sd and rtemp
+// are read in halos that other CTAs own, so they ping-pong between launches;
 // utemp is read and written only at owned cells (its halo values are never
 // stored) and is updated in place.  Every value is computed with the
-// operations of k_pp_step in the same order, so T fused steps give the
-// bits of T single steps.
+// operations of k_pp_step in the same order, so T fused steps give the bits
+// of T single steps.
 constexpr int kFusedThreads = 256;
 constexpr int kFusedMax = 4;       // most steps fused into one pass
 
@@ -574,30 +578,45 @@ struct PpFusedArgs {
     double *z64;                    // LAST: z = utemp in FP64
 };
 
+// coefficient arrays staged per strip: Kx, Ky, then cp, bfp (block) or Mi (diag)
+template <int PC>
+__host__ __device__ constexpr int fused_narr() {
+    return PC == TL_PREC_JAC_BLOCK ? 4 : (PC == TL_PREC_JAC_DIAG ? 3 : 2);
+}
+
+// shared-memory rows hold one value per thread plus a zero at each end, so
+// the west / east neighbours of the band's edge threads read zeros
+constexpr int kFusedRow = kFusedThreads + 2;
+
+template <int T, int PC>
+__host__ __device__ constexpr size_t fused_smem() {
+    return sizeof(float) * kFusedRow * 4 * (2 * T + (T + 1) * fused_narr<PC>());
+}
+
 template <int T, int PC, bool LAST>
-__global__ void __launch_bounds__(kFusedThreads) k_pp_fused(PpFusedArgs a, const DevScalars *__restrict__ sc) {
+__global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, const DevScalars *__restrict__ sc) {
     if (*(volatile const int *)&sc->done) return;
-    __shared__ float xs[T][2][4][kFusedThreads];
+    constexpr int NT = kFusedThreads;
+    constexpr int SR = kFusedRow;  // shared-memory row stride
+    constexpr int NA = fused_narr<PC>();
+    constexpr int R = T + 1;  // ring slots
+    extern __shared__ float smem[];
     const int tid = threadIdx.x;
+    float *const xsb = smem + 1;              // [T][2][4][SR]: sd rows by level and parity
+    float *const cfb = smem + 1 + 8 * T * SR; // [R][NA][4][SR]: coefficients by strip slot
     const int col = blockIdx.x * a.band - T + tid;
     const bool incol = col >= 0 && col < a.nx;
     const bool own = incol && tid >= T && tid < T + a.band;
     const int nstrips = (a.ny + 3) >> 2;
     const int sb = blockIdx.y * a.seg;
     const int se = min(sb + a.seg, nstrips);
-    const int64_t P = a.pitch;
     float al[T], be[T];
 #pragma unroll
     for (int t = 0; t < T; ++t) {
         al[t] = (float)a.alphas[a.step0 + t - 1];
         be[t] = (float)a.betas[a.step0 + t - 1];
     }
-#pragma unroll
-    for (int l = 0; l < T; ++l)
-#pragma unroll
-        for (int p = 0; p < 2; ++p)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) xs[l][p][k][tid] = 0.f;
+    for (int k = tid; k < (8 * T + 4 * R * NA) * SR; k += NT) smem[k] = 0.f;
     // per producer level l < T: its output strip of the previous iteration
     // (sd, rtemp, utemp) and the last sd row of the one before
     float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
@@ -607,80 +626,99 @@ __global__ void __launch_bounds__(kFusedThreads) k_pp_fused(PpFusedArgs a, const
 #pragma unroll
         for (int k = 0; k < 4; ++k) sdP[l][k] = rtP[l][k] = utP[l][k] = 0.f;
     }
-    // level 0 loads, one strip ahead
-    float ldS[4], ldR[4], ldU[4];
+    // level 0 loads, one strip ahead (32-bit offsets: a field has < 2^31 elements)
+    float ldS[4], ldR[4], ldU[4], ldC[NA][4];
+    const int cbase = col + a.h;
     auto load = [&](int s) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int row = 4 * s + k;
             const bool v = incol && s >= 0 && row < a.ny;
-            const int64_t i = (int64_t)(col + a.h) + (int64_t)(row + a.h) * P;
+            const int i = cbase + (row + a.h) * a.pitch;
             ldS[k] = v ? a.sd_in[i] : 0.f;
             ldR[k] = v ? a.rt_in[i] : 0.f;
             ldU[k] = v ? a.utemp[i] : 0.f;
+            ldC[0][k] = v ? __ldg(&a.kx[i]) : 0.f;
+            ldC[1][k] = v ? __ldg(&a.ky[i]) : 0.f;
+            if (PC == TL_PREC_JAC_BLOCK) {
+                ldC[2][k] = v ? __ldg(&a.cp[i]) : 0.f;
+                ldC[3][k] = v ? __ldg(&a.bfp[i]) : 0.f;
+            } else if (PC == TL_PREC_JAC_DIAG) {
+                ldC[NA - 1][k] = v ? __ldg(&a.mi[i]) : 0.f;
+            }
         }
     };
+    auto slot_of = [](int q) { return (q + 8 * R) % R; };  // q >= -2T >= -8
     load(sb - T);
     __syncthreads();
     for (int s = sb - T; s < se + T; ++s) {
         float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
+        {
+            float *cf = cfb + slot_of(s) * NA * 4 * SR + tid;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            cS[k] = ldS[k];
-            cR[k] = ldR[k];
-            cU[k] = ldU[k];
-            xs[0][s & 1][k][tid] = ldS[k];
+            for (int k = 0; k < 4; ++k) {
+                cS[k] = ldS[k];
+                cR[k] = ldR[k];
+                cU[k] = ldU[k];
+                xsb[((0 * 2 + (s & 1)) * 4 + k) * SR + tid] = ldS[k];
+#pragma unroll
+                for (int r = 0; r < NA; ++r) cf[(r * 4 + k) * SR] = ldC[r][k];
+            }
         }
         if (s + 1 < se + T) load(s + 1);
 #pragma unroll
         for (int t = 1; t <= T; ++t) {
             const int q = s - t;
             const int m = (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
-            const int64_t i0 = (int64_t)(col + a.h) + (int64_t)(4 * q + a.h) * P;
+            const float *cf = cfb + slot_of(q) * NA * 4 * SR + tid;       // this strip
+            const float *cn = cfb + slot_of(q + 1) * NA * 4 * SR + tid;   // the strip above it
+            const float *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * 4 * SR + tid;
             const float(&x0)[4] = sdP[t - 1];
-            const int pr = (s - 1) & 1;
-            float oS[4], oR[4], oU[4], z[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                oS[k] = oR[k] = oU[k] = z[k] = 0.f;
-                if (k < m) {
-                    const int64_t i = i0 + (int64_t)k * P;
-                    const float c = x0[k];
-                    const float n = k < 3 ? x0[k + 1] : cS[0];
-                    const float sv = k > 0 ? x0[k - 1] : sdL[t - 1];
-                    const float w = tid > 0 ? xs[t - 1][pr][k][tid - 1] : 0.f;
-                    const float e = tid < kFusedThreads - 1 ? xs[t - 1][pr][k][tid + 1] : 0.f;
-                    oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, w, e, __ldg(&a.ky[i + P]), __ldg(&a.ky[i]),
-                                                       __ldg(&a.kx[i + 1]), __ldg(&a.kx[i]));
-                }
-            }
-            if constexpr (PC == TL_PREC_JAC_BLOCK) {
-                // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
-                // z_k = dp_k - cp_k z_{k+1}
+            float oS[4], oR[4], oU[4];
+            // one inner step on the strip's first mm rows (mm == 4: no row tests)
+            auto step = [&](const int mm) {
+                float z[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    if (k < m) {
-                        const int64_t i = i0 + (int64_t)k * P;
-                        const float bf = __ldg(&a.bfp[i]);
-                        z[k] = k == 0 ? oR[0] * bf : fmaf(__ldg(&a.ky[i]), z[k - 1], oR[k]) * bf;
+                    oS[k] = oR[k] = oU[k] = z[k] = 0.f;
+                    if (k < mm) {
+                        const float c = x0[k];
+                        const float n = k < 3 ? x0[k + 1] : cS[0];
+                        const float sv = k > 0 ? x0[k - 1] : sdL[t - 1];
+                        const float kyn = k < 3 ? cf[(1 * 4 + k + 1) * SR] : cn[(1 * 4 + 0) * SR];
+                        oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, xp[k * SR - 1], xp[k * SR + 1], kyn,
+                                                           cf[(1 * 4 + k) * SR], cf[(0 * 4 + k) * SR + 1],
+                                                           cf[(0 * 4 + k) * SR]);
                     }
                 }
+                if constexpr (PC == TL_PREC_JAC_BLOCK) {
+                    // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
+                    // z_k = dp_k - cp_k z_{k+1}
 #pragma unroll
-                for (int k = 2; k >= 0; --k)
-                    if (k < m - 1) z[k] = fmaf(-__ldg(&a.cp[i0 + (int64_t)k * P]), z[k + 1], z[k]);
-            } else {
+                    for (int k = 0; k < 4; ++k) {
+                        if (k < mm) {
+                            const float bf = cf[(3 * 4 + k) * SR];
+                            z[k] = k == 0 ? oR[0] * bf : fmaf(cf[(1 * 4 + k) * SR], z[k - 1], oR[k]) * bf;
+                        }
+                    }
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if (k < m)
-                        z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * __ldg(&a.mi[i0 + (int64_t)k * P]) : oR[k];
-            }
+                    for (int k = 2; k >= 0; --k)
+                        if (k < mm - 1) z[k] = fmaf(-cf[(2 * 4 + k) * SR], z[k + 1], z[k]);
+                } else {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (k < m) {
-                    oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
-                    oU[k] = utP[t - 1][k] + oS[k];
+                    for (int k = 0; k < 4; ++k)
+                        if (k < mm) z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * cf[((NA - 1) * 4 + k) * SR] : oR[k];
                 }
-            }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (k < mm) {
+                        oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
+                        oU[k] = utP[t - 1][k] + oS[k];
+                    }
+                }
+            };
+            if (m == 4) step(4);
+            else step(m);
             // level t-1 has been consumed: its output of this iteration moves in
             sdL[t - 1] = sdP[t - 1][3];
 #pragma unroll
@@ -694,15 +732,16 @@ __global__ void __launch_bounds__(kFusedThreads) k_pp_fused(PpFusedArgs a, const
             }
             if (t < T) {
 #pragma unroll
-                for (int k = 0; k < 4; ++k) xs[t][s & 1][k][tid] = oS[k];
+                for (int k = 0; k < 4; ++k) xsb[((t * 2 + (s & 1)) * 4 + k) * SR + tid] = oS[k];
             } else if (own && q >= sb && q < se) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     if (k < m) {
-                        const int64_t i = i0 + (int64_t)k * P;
+                        const int row = 4 * q + k;
                         if (LAST) {
-                            a.z64[(int64_t)(col + a.h) + (int64_t)(4 * q + k + a.h) * a.pitch64] = (double)oU[k];
+                            a.z64[(int64_t)cbase + (int64_t)(row + a.h) * a.pitch64] = (double)oU[k];
                         } else {
+                            const int i = cbase + (row + a.h) * a.pitch;
                             a.sd_out[i] = oS[k];
                             a.rt_out[i] = oR[k];
                             a.utemp[i] = oU[k];
@@ -788,6 +827,50 @@ struct BodyUpdateU {  // u += d (FP64)
             if (k < m) {
                 const int64_t i = b64 + (int64_t)k * pitch64;
                 u[i] = u[i] + (double)d[b32 + (int64_t)k * pitch32];
+            }
+    }
+};
+
+// PPCG outer update fused with the start of the FP32 inner steps:
+// u += alpha p, r -= alpha w, z = M^-1 r (FP64, as BodyCgUr of tl_kernels.cu),
+// then rtemp = r, sd = utemp = z / theta in FP32 (as k_pp_init) -- z itself is
+// not stored, the inner steps overwrite it
+template <int PC>
+struct BodyPpUr {
+    const double *dg, *p, *w, *mi, *ky, *cp, *bfp;
+    double *u, *r;
+    float *sd, *rtemp, *utemp;
+    int pitch32, pitch64;
+    double alpha, theta_r;
+    __device__ void setup(DevScalars *sc) {
+        alpha = sc->alpha;
+        theta_r = 1.0 / sc->theta;
+    }
+    __device__ void operator()(int64_t b32, int64_t b64, int m, CSum &) const {
+        double rv[4], zv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = b64 + (int64_t)k * pitch64;
+                u[i] = fma(alpha, p[i], u[i]);
+                rv[k] = fma(-alpha, w[i], r[i]);
+                r[i] = rv[k];
+            }
+        if (PC == TL_PREC_JAC_BLOCK) {
+            strip_block_solve(dg, ky, cp, bfp, pitch64, b64, m, rv, zv);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < m) zv[k] = PC == TL_PREC_JAC_DIAG ? rv[k] * mi[b64 + (int64_t)k * pitch64] : rv[k];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t j = b32 + (int64_t)k * pitch32;
+                rtemp[j] = (float)rv[k];
+                const float sv = (float)(zv[k] * theta_r);
+                sd[j] = sv;
+                utemp[j] = sv;
             }
     }
 };
@@ -891,10 +974,22 @@ int mixed_ppcg_prepare(Chunk *c) {
     });
 }
 
+template <int T, int PC, bool LAST>
+void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, const DevScalars *sc) {
+    constexpr size_t bytes = fused_smem<T, PC>();
+    static bool configured = false;  // the attribute belongs to the kernel: set once
+    if (!configured) {
+        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        configured = true;
+    }
+    k_pp_fused<T, PC, LAST><<<grid, kFusedThreads, bytes, s>>>(a, sc);
+}
+
 template <int T, int PC>
 void launch_fused(dim3 grid, cudaStream_t s, const PpFusedArgs &a, bool last, const DevScalars *sc) {
-    if (last) k_pp_fused<T, PC, true><<<grid, kFusedThreads, 0, s>>>(a, sc);
-    else k_pp_fused<T, PC, false><<<grid, kFusedThreads, 0, s>>>(a, sc);
+    if (last) launch_fused1<T, PC, true>(grid, s, a, sc);
+    else launch_fused1<T, PC, false>(grid, s, a, sc);
 }
 
 template <int T>
@@ -908,27 +1003,17 @@ void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bo
 // With c->inner_fuse > 1 the steps run as ceil(inner / inner_fuse) passes of
 // k_pp_fused (sizes as even as possible, larger first); otherwise one
 // k_pp_step per step.
-int mixed_ppcg_inner(Chunk *c) {
+namespace {
+
+// the inner steps proper, from sd[0], rtemp, utemp to z (FP64)
+int inner_steps(Chunk *c) {
     Mixed *mx = mixed_of(c);
     const int inner = c->cfg.ppcg_inner_steps;
-    if (!mx || inner < 1) {
-        set_error("mixed PPCG needs tl_ppcg_inner_steps >= 1 and a prepared chunk");
-        return TL_ERR_STATE;
-    }
     const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
     const unsigned grid = (unsigned)mx->vtiles;
     cudaStream_t s = c->stream;
     const int pc = c->cfg.precond;
     int rc;
-    if ((rc = launch_v(c, "mixed_pp_init", [&] {
-             if (pc == TL_PREC_NONE)
-                 k_pp_init<false><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, c->r, c->z, mx->sd[0], mx->rtemp,
-                                                                 mx->utemp, c->sc);
-             else
-                 k_pp_init<true><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, c->r, c->z, mx->sd[0], mx->rtemp,
-                                                                mx->utemp, c->sc);
-         })))
-        return rc;
     const int fuse = c->inner_fuse < 1 ? 1 : (c->inner_fuse > kFusedMax ? kFusedMax : c->inner_fuse);
     if (fuse > 1) {
         float *rt[2] = {mx->rtemp, mx->rtemp2};
@@ -999,6 +1084,50 @@ int mixed_ppcg_inner(Chunk *c) {
         if (rc) return rc;
     }
     return TL_OK;
+}
+
+bool inner_ready(Chunk *c) {
+    if (!mixed_of(c) || c->cfg.ppcg_inner_steps < 1) {
+        set_error("mixed PPCG needs tl_ppcg_inner_steps >= 1 and a prepared chunk");
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+int mixed_ppcg_inner(Chunk *c) {
+    if (!inner_ready(c)) return TL_ERR_STATE;
+    Mixed *mx = mixed_of(c);
+    const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
+    const unsigned grid = (unsigned)mx->vtiles;
+    cudaStream_t s = c->stream;
+    int rc;
+    if ((rc = launch_v(c, "mixed_pp_init", [&] {
+             if (c->cfg.precond == TL_PREC_NONE)
+                 k_pp_init<false><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, c->r, c->z, mx->sd[0], mx->rtemp,
+                                                                 mx->utemp, c->sc);
+             else
+                 k_pp_init<true><<<grid, kBlockThreads, 0, s>>>(g, c->pitch, c->r, c->z, mx->sd[0], mx->rtemp,
+                                                                mx->utemp, c->sc);
+         })))
+        return rc;
+    return inner_steps(c);
+}
+
+int mixed_ppcg_ur_inner(Chunk *c) {
+    if (!inner_ready(c)) return TL_ERR_STATE;
+    Mixed *mx = mixed_of(c);
+    int rc;
+#define TL_PP_UR(PC)                                                                                       \
+    BodyPpUr<PC>{c->diag, c->p, c->w, c->mi, c->ky, c->cp, c->bfp, c->u, c->r, mx->sd[0], mx->rtemp,      \
+                 mx->utemp, c->pitch, c->pitch, 0.0, 0.0}
+    if (c->cfg.precond == TL_PREC_JAC_BLOCK) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_BLOCK), kInNone, true);
+    else if (c->cfg.precond == TL_PREC_JAC_DIAG) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_DIAG), kInNone, true);
+    else rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_NONE), kInNone, true);
+#undef TL_PP_UR
+    if (rc) return rc;
+    return inner_steps(c);
 }
 
 void mixed_free(Chunk *c) {

@@ -74,10 +74,13 @@ int body_cg(Chunk *c) {
 int body_ppcg(Chunk *c) {
     int rc;
     if ((rc = launch_cg_w(c, kEpiPw, true))) return rc;
-    if ((rc = launch_copy(c, c->r_store, c->r, true))) return rc;
-    if ((rc = launch_ppcg_zr(c, kEpiPpcgZr, true))) return rc;
-    if ((rc = launch_cg_ur(c, 0.0, kEpiNone, true))) return rc;
-    if ((rc = ppcg_inner_steps(c, true))) return rc;
+    if ((rc = launch_ppcg_store_zr(c, kEpiPpcgZr, true))) return rc;
+    if (c->cfg.precision == TL_PRECISION_MIXED) {
+        if ((rc = mixed_ppcg_ur_inner(c))) return rc;
+    } else {
+        if ((rc = launch_cg_ur(c, 0.0, kEpiNone, true))) return rc;
+        if ((rc = ppcg_inner_steps(c, true))) return rc;
+    }
     if ((rc = launch_ppcg_rrn(c, kEpiPpcgRrn, true))) return rc;
     if ((rc = launch_ppcg_p(c, 0.0, kEpiFinishNoSwitch, true))) return rc;
     return halo(c, TL_FIELD_P, 1);
