@@ -82,6 +82,7 @@ BYTES_PER_CELL = {
     "ppcg_p": 24,        # read z, p; write p
     "copy": 16,          # read src; write dst
     "ppcg_store_zr": 24,  # read r, z; write r_store
+    "ppcg_w_zr": 64,     # read p, Kx, Ky, diag, r, z; write w, r_store
     "ppcg_rrn": 24,      # read r, r_store, z
     # mixed precision: FP32 inner iteration (4-byte elements)
     "mixed_w": 16,       # read p, Kx, Ky; write w
@@ -91,6 +92,15 @@ BYTES_PER_CELL = {
     "mixed_update_u": 20,  # read u (FP64), d; write u (FP64)
     "mixed_convert": 40,   # read Kx, Ky (FP64); write Kx, Ky, Mi (FP32)
     "mixed_pp_init": 28,   # read r, z (FP64); write sd, rtemp, utemp
+}
+
+
+# DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
+# launch / cells), for the kernels that can dominate the default workload;
+# scaled to a launch by the cells it processes
+TRAFFIC_PER_CELL = {
+    "mixed_pp_fused": 37.5,   # k_pp_fused<3, jac_block> at 4096^2: 514.8 + 115.3 MB
+    "cg_w": 39.6,             # BodyCgW at 4096^2: 545.5 + 119.4 MB
 }
 
 
@@ -364,7 +374,9 @@ def run_ours(args):
     peak = peak or 6800.0
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_src,
-                "traffic": args.traffic_per_launch,
+                "traffic": (args.traffic_per_launch if args.traffic_per_launch is not None else
+                            (TRAFFIC_PER_CELL[dom] * cells if dom in TRAFFIC_PER_CELL and
+                             (dom != "mixed_pp_fused" or args.precond == "jac_block") else None)),
                 "bytes_per_cell": bpc, "launch_ms": dom_launch_ms,
                 "kernel_share": {k2: round(v["ms"] / total_kms, 4) for k2, v in
                                  sorted(kernels.items(), key=lambda kv: -kv[1]["ms"])},

@@ -68,6 +68,7 @@ enum Epilogue : int {
     kEpiJacobi,       // error = sum |du|, exit test
     kEpiPw,           // pw = p.w
     kEpiFinishNoSwitch,  // exit test once Chebyshev/PPCG has taken over
+    kEpiPwZr,         // pw = sum 0, rro = sum 1, alpha = rro/pw (PPCG outer)
 };
 
 struct Geo {
@@ -185,6 +186,7 @@ int launch_copy(Chunk *c, double *dst, const double *src, bool fast);
 int launch_ppcg_rrn(Chunk *c, int epi, bool fast);
 int launch_ppcg_zr(Chunk *c, int epi, bool fast);
 int launch_ppcg_store_zr(Chunk *c, int epi, bool fast);  // r_store = r + ppcg_zr
+int launch_ppcg_w_store_zr(Chunk *c, bool fast);         // cg_w + ppcg_store_zr, one pass
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast);
 int launch_jacobi(Chunk *c, int epi, bool fast);
 int launch_finalise(Chunk *c);

@@ -96,6 +96,11 @@ __device__ void run_epilogue(const RedCtx &red, const double *tot, int nv) {
         s->rro = tot[0];
         s->alpha = s->rro / s->pw;
         break;
+    case kEpiPwZr:
+        s->pw = tot[0];
+        s->rro = tot[1];
+        s->alpha = s->rro / s->pw;
+        break;
     case kEpiPpcgRrn:
         s->rrn = tot[0];
         s->beta = s->rrn / s->rro;
@@ -644,6 +649,29 @@ struct BodyCopy {
     }
 };
 
+struct BodyCgWStoreZr {  // BodyCgW and BodyStoreZr in one pass: w = A p, r_store = r;
+                         // sums p.w and r.z, each in its own kernel's order
+    const double *dg;
+    const double *p, *kx, *ky, *r, *z;
+    double *w, *r_store;
+    int pitch;
+    __device__ void setup() {}
+    __device__ void operator()(int64_t base, int m, double (&acc)[2]) const {
+        double xc[4], ax[4];
+        strip_apply(kx, ky, dg, pitch, base, m, LoadX{p}, xc, ax);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = base + (int64_t)k * pitch;
+                w[i] = ax[k];
+                acc[0] = fma(xc[k], ax[k], acc[0]);
+                const double rv = r[i];
+                r_store[i] = rv;
+                acc[1] = fma(rv, z[i], acc[1]);
+            }
+    }
+};
+
 struct BodyStoreZr {  // r_store = r and sum r.z in one pass (tea_leaf_ppcg.cuknl:302-313 + the
                       // r.z norm); the sum is BodyNorm{r, z}'s, in the same order
     const double *r, *z;
@@ -1060,6 +1088,11 @@ int launch_ppcg_rrn(Chunk *c, int epi, bool fast) {
 int launch_ppcg_zr(Chunk *c, int epi, bool fast) {
     BodyNorm b{c->r, c->z, c->pitch};
     return run<1>(c, "ppcg_zr", b, epi, fast);
+}
+
+int launch_ppcg_w_store_zr(Chunk *c, bool fast) {
+    BodyCgWStoreZr b{c->diag, c->p, c->kx, c->ky, c->r, c->z, c->w, c->r_store, c->pitch};
+    return run<2>(c, "ppcg_w_zr", b, kEpiPwZr, fast);
 }
 
 int launch_ppcg_store_zr(Chunk *c, int epi, bool fast) {

@@ -73,8 +73,7 @@ int body_cg(Chunk *c) {
 
 int body_ppcg(Chunk *c) {
     int rc;
-    if ((rc = launch_cg_w(c, kEpiPw, true))) return rc;
-    if ((rc = launch_ppcg_store_zr(c, kEpiPpcgZr, true))) return rc;
+    if ((rc = launch_ppcg_w_store_zr(c, true))) return rc;
     if (c->cfg.precision == TL_PRECISION_MIXED) {
         if ((rc = mixed_ppcg_ur_inner(c))) return rc;
     } else {
