@@ -112,9 +112,9 @@ def bytes_per_cell(kernel, precond):
         # before the last)
         return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
     if kernel == "mixed_pp_ur":
-        # read u, p, w, r (FP64) + the preconditioner (Mi; or diag, Ky, cp,
+        # read u, p, w, r (FP64) + the FP32 preconditioner (Mi; or Ky, cp,
         # bfp); write u, r (FP64) and rtemp, sd, utemp (FP32)
-        return {"none": 60, "jac_diag": 68, "jac_block": 92}[precond]
+        return {"none": 60, "jac_diag": 64, "jac_block": 72}[precond]
     if kernel == "mixed_pp_fused":
         # the same arrays once per pass of several inner steps
         return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]

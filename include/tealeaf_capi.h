@@ -183,8 +183,9 @@ int tl_set_profiling(tl_chunk_t *ch, int on);
 int tl_profile_reset(tl_chunk_t *ch);
 /* mixed-precision PPCG: run `steps` (1..4) FP32 inner steps per pass over
  * HBM (temporal blocking; 1 = one kernel per inner step), each CTA taking
- * `seg_strips` 4-row strips of a column band.  Results are bitwise the same
- * for every setting; only the speed changes.  Default 4 and 64. */
+ * `seg_strips` 4-row strips of a column band (0: chosen from the grid size,
+ * one wave of CTAs).  Results are bitwise the same for every setting; only
+ * the speed changes.  Default 4 and 0. */
 int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips);
 int tl_profile_read(tl_chunk_t *ch, int idx, const char **name, long long *launches, double *ms);
 /* the process-wide chunk the reference-named entry points act on */

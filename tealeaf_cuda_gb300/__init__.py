@@ -246,8 +246,9 @@ class Chunk:
     def set_dt(self, dt):
         _check(load().tl_set_dt(self._h, dt), "tl_set_dt")
 
-    def set_inner_fusion(self, steps, seg_strips=32):
-        """FP32 PPCG inner steps per HBM pass (1..4) and strips per CTA segment"""
+    def set_inner_fusion(self, steps, seg_strips=0):
+        """FP32 PPCG inner steps per HBM pass (1..4) and strips per CTA
+        segment (0: automatic)"""
         _check(load().tl_set_inner_fusion(self._h, steps, seg_strips), "tl_set_inner_fusion")
 
     def timestep(self):

@@ -122,6 +122,7 @@ static int chunk_alloc(const tl_config_t *cfg, Chunk **out) {
     c->inner_seg = kInnerSegDefault;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    c->sms = sms > 0 ? sms : 152;
     c->grid_red = sms > 0 ? sms * 4 : 512;
     if (c->grid_red > kMaxRedBlocks) c->grid_red = kMaxRedBlocks;
 
@@ -522,8 +523,8 @@ int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips) {
         set_error("tl_set_inner_fusion: no chunk");
         return TL_ERR_STATE;
     }
-    if (steps < 1 || steps > 4 || seg_strips < 1) {
-        set_error("tl_set_inner_fusion: steps must be 1..4 and seg_strips >= 1 (got %d, %d)", steps, seg_strips);
+    if (steps < 1 || steps > 4 || seg_strips < 0) {
+        set_error("tl_set_inner_fusion: steps must be 1..4 and seg_strips >= 0 (got %d, %d)", steps, seg_strips);
         return TL_ERR_ARG;
     }
     Chunk *c = ch->c;

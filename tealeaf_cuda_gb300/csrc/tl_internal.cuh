@@ -126,7 +126,8 @@ struct Chunk {
     // mixed precision state (allocated on first use)
     void *mixed;
     int inner_fuse;              // FP32 PPCG inner steps per HBM pass (1: one kernel per step)
-    int inner_seg;               // 4-row strips per CTA segment of the fused inner kernel
+    int inner_seg;               // 4-row strips per CTA segment of the fused inner kernel (0: automatic)
+    int sms;                     // multiprocessors of the device
     // learned warm start model and buffers (tl_warm.cu)
     void *warm;
     double rx, ry;
@@ -220,7 +221,7 @@ int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
 int mixed_ppcg_ur_inner(Chunk *c); // the outer u/r update fused with the inner start, then the steps
 void drop_graphs(Chunk *c);        // after a change that captured graphs depend on
 constexpr int kInnerFuseDefault = 4;
-constexpr int kInnerSegDefault = 64;
+constexpr int kInnerSegDefault = 0;
 // warm starts (tl_warm.cu)
 void warm_free(Chunk *c);
 void warm_reset(Chunk *c);                // forget u^(n-1) (tl_start)

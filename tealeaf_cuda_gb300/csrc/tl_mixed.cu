@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 // stored) and is updated in place.  Every value is computed with the
 // operations of k_pp_step in the same order, so T fused steps give the bits
 // of T single steps.
-constexpr int kFusedThreads = 256;
+constexpr int kFusedThreads = 224;  // 7 warps: two CTAs' shared memory fit an SM at T = 4
 constexpr int kFusedMax = 4;       // most steps fused into one pass
 
 struct PpFusedArgs {
@@ -578,7 +578,8 @@ struct PpFusedArgs {
     double *z64;                    // LAST: z = utemp in FP64
 };
 
-// coefficient arrays staged per strip: Kx, Ky, then cp, bfp (block) or Mi (diag)
+// coefficient arrays staged per strip: Kx, Ky, then cp, bfp (block) or Mi (diag),
+// packed per cell as one float4 {Kx, Ky, cp | Mi, bfp}
 template <int PC>
 __host__ __device__ constexpr int fused_narr() {
     return PC == TL_PREC_JAC_BLOCK ? 4 : (PC == TL_PREC_JAC_DIAG ? 3 : 2);
@@ -590,7 +591,7 @@ constexpr int kFusedRow = kFusedThreads + 2;
 
 template <int T, int PC>
 __host__ __device__ constexpr size_t fused_smem() {
-    return sizeof(float) * kFusedRow * 4 * (2 * T + (T + 1) * fused_narr<PC>());
+    return sizeof(float4) * kFusedRow * 4 * (T + 1) + sizeof(float) * kFusedRow * 4 * 2 * T;
 }
 
 template <int T, int PC, bool LAST>
@@ -600,10 +601,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
     constexpr int SR = kFusedRow;  // shared-memory row stride
     constexpr int NA = fused_narr<PC>();
     constexpr int R = T + 1;  // ring slots
-    extern __shared__ float smem[];
+    extern __shared__ float4 smem4[];
     const int tid = threadIdx.x;
-    float *const xsb = smem + 1;              // [T][2][4][SR]: sd rows by level and parity
-    float *const cfb = smem + 1 + 8 * T * SR; // [R][NA][4][SR]: coefficients by strip slot
+    float4 *const cfb = smem4 + 1;            // [R][4][SR]: coefficients by strip slot
+    float *const xsb = reinterpret_cast<float *>(smem4 + R * 4 * SR) + 1;  // [T][2][4][SR]: sd rows
     const int col = blockIdx.x * a.band - T + tid;
     const bool incol = col >= 0 && col < a.nx;
     const bool own = incol && tid >= T && tid < T + a.band;
@@ -616,7 +617,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
         al[t] = (float)a.alphas[a.step0 + t - 1];
         be[t] = (float)a.betas[a.step0 + t - 1];
     }
-    for (int k = tid; k < (8 * T + 4 * R * NA) * SR; k += NT) smem[k] = 0.f;
+    {
+        float *z = reinterpret_cast<float *>(smem4);
+        for (int k = tid; k < (16 * R + 8 * T) * SR; k += NT) z[k] = 0.f;
+    }
     // per producer level l < T: its output strip of the previous iteration
     // (sd, rtemp, utemp) and the last sd row of the one before
     float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
@@ -654,15 +658,15 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
     for (int s = sb - T; s < se + T; ++s) {
         float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
         {
-            float *cf = cfb + slot_of(s) * NA * 4 * SR + tid;
+            float4 *cf = cfb + slot_of(s) * 4 * SR + tid;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 cS[k] = ldS[k];
                 cR[k] = ldR[k];
                 cU[k] = ldU[k];
                 xsb[((0 * 2 + (s & 1)) * 4 + k) * SR + tid] = ldS[k];
-#pragma unroll
-                for (int r = 0; r < NA; ++r) cf[(r * 4 + k) * SR] = ldC[r][k];
+                cf[k * SR] = make_float4(ldC[0][k], ldC[1][k], NA > 2 ? ldC[NA > 2 ? 2 : 0][k] : 0.f,
+                                         NA > 3 ? ldC[NA > 3 ? 3 : 0][k] : 0.f);
             }
         }
         if (s + 1 < se + T) load(s + 1);
@@ -670,8 +674,8 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
         for (int t = 1; t <= T; ++t) {
             const int q = s - t;
             const int m = (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
-            const float *cf = cfb + slot_of(q) * NA * 4 * SR + tid;       // this strip
-            const float *cn = cfb + slot_of(q + 1) * NA * 4 * SR + tid;   // the strip above it
+            const float4 *cf = cfb + slot_of(q) * 4 * SR + tid;       // this strip
+            const float4 *cn = cfb + slot_of(q + 1) * 4 * SR + tid;   // the strip above it
             const float *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * 4 * SR + tid;
             const float(&x0)[4] = sdP[t - 1];
             float oS[4], oR[4], oU[4];
@@ -685,10 +689,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
                         const float c = x0[k];
                         const float n = k < 3 ? x0[k + 1] : cS[0];
                         const float sv = k > 0 ? x0[k - 1] : sdL[t - 1];
-                        const float kyn = k < 3 ? cf[(1 * 4 + k + 1) * SR] : cn[(1 * 4 + 0) * SR];
-                        oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, xp[k * SR - 1], xp[k * SR + 1], kyn,
-                                                           cf[(1 * 4 + k) * SR], cf[(0 * 4 + k) * SR + 1],
-                                                           cf[(0 * 4 + k) * SR]);
+                        const float4 cc = cf[k * SR];
+                        const float kyn = k < 3 ? cf[(k + 1) * SR].y : cn[0].y;
+                        oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, xp[k * SR - 1], xp[k * SR + 1], kyn, cc.y,
+                                                           cf[k * SR + 1].x, cc.x);
                     }
                 }
                 if constexpr (PC == TL_PREC_JAC_BLOCK) {
@@ -697,17 +701,17 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         if (k < mm) {
-                            const float bf = cf[(3 * 4 + k) * SR];
-                            z[k] = k == 0 ? oR[0] * bf : fmaf(cf[(1 * 4 + k) * SR], z[k - 1], oR[k]) * bf;
+                            const float4 cc = cf[k * SR];
+                            z[k] = k == 0 ? oR[0] * cc.w : fmaf(cc.y, z[k - 1], oR[k]) * cc.w;
                         }
                     }
 #pragma unroll
                     for (int k = 2; k >= 0; --k)
-                        if (k < mm - 1) z[k] = fmaf(-cf[(2 * 4 + k) * SR], z[k + 1], z[k]);
+                        if (k < mm - 1) z[k] = fmaf(-cf[k * SR].z, z[k + 1], z[k]);
                 } else {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        if (k < mm) z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * cf[((NA - 1) * 4 + k) * SR] : oR[k];
+                        if (k < mm) z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * cf[k * SR].z : oR[k];
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
@@ -832,43 +836,55 @@ struct BodyUpdateU {  // u += d (FP64)
 };
 
 // PPCG outer update fused with the start of the FP32 inner steps:
-// u += alpha p, r -= alpha w, z = M^-1 r (FP64, as BodyCgUr of tl_kernels.cu),
-// then rtemp = r, sd = utemp = z / theta in FP32 (as k_pp_init) -- z itself is
-// not stored, the inner steps overwrite it
+// u += alpha p, r -= alpha w (FP64, as BodyCgUr of tl_kernels.cu), then
+// rtemp = r, z = M^-1 r and sd = utemp = z / theta in FP32 (as k_pp_init):
+// z only seeds the FP32 polynomial preconditioner, so M^-1 uses the FP32
+// operator copies (the block solve of k_pp_step, 1/diag in bfp's first row)
 template <int PC>
 struct BodyPpUr {
-    const double *dg, *p, *w, *mi, *ky, *cp, *bfp;
+    const double *p, *w;
     double *u, *r;
+    const float *mi, *ky, *cp, *bfp;
     float *sd, *rtemp, *utemp;
     int pitch32, pitch64;
-    double alpha, theta_r;
+    double alpha;
+    float theta_r;
     __device__ void setup(DevScalars *sc) {
         alpha = sc->alpha;
-        theta_r = 1.0 / sc->theta;
+        theta_r = (float)(1.0 / sc->theta);
     }
     __device__ void operator()(int64_t b32, int64_t b64, int m, CSum &) const {
-        double rv[4], zv[4];
+        float rf[4], zf[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t i = b64 + (int64_t)k * pitch64;
                 u[i] = fma(alpha, p[i], u[i]);
-                rv[k] = fma(-alpha, w[i], r[i]);
-                r[i] = rv[k];
+                const double rv = fma(-alpha, w[i], r[i]);
+                r[i] = rv;
+                rf[k] = (float)rv;
             }
         if (PC == TL_PREC_JAC_BLOCK) {
-            strip_block_solve(dg, ky, cp, bfp, pitch64, b64, m, rv, zv);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k < m) {
+                    const int64_t j = b32 + (int64_t)k * pitch32;
+                    zf[k] = k == 0 ? rf[0] * bfp[j] : fmaf(ky[j], zf[k - 1], rf[k]) * bfp[j];
+                }
+#pragma unroll
+            for (int k = 2; k >= 0; --k)
+                if (k < m - 1) zf[k] = fmaf(-cp[b32 + (int64_t)k * pitch32], zf[k + 1], zf[k]);
         } else {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (k < m) zv[k] = PC == TL_PREC_JAC_DIAG ? rv[k] * mi[b64 + (int64_t)k * pitch64] : rv[k];
+                if (k < m) zf[k] = PC == TL_PREC_JAC_DIAG ? rf[k] * mi[b32 + (int64_t)k * pitch32] : rf[k];
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t j = b32 + (int64_t)k * pitch32;
-                rtemp[j] = (float)rv[k];
-                const float sv = (float)(zv[k] * theta_r);
+                rtemp[j] = rf[k];
+                const float sv = zf[k] * theta_r;
                 sd[j] = sv;
                 utemp[j] = sv;
             }
@@ -1029,9 +1045,17 @@ int inner_steps(Chunk *c) {
             a.h = c->h;
             a.pitch = c->pitch;
             a.pitch64 = c->pitch;
-            a.seg = c->inner_seg;
-            if ((nstrips + a.seg - 1) / a.seg > 65535) a.seg = (nstrips + 65534) / 65535;
             a.band = kFusedThreads - 2 * T;
+            a.seg = c->inner_seg;
+            if (a.seg < 1) {
+                // automatic: one wave of 2 CTAs per SM with the longest segments
+                // (each segment recomputes 2T strips of pipeline warm-up)
+                const int bands = (c->nx + a.band - 1) / a.band;
+                const int per_col = (2 * c->sms) / bands > 1 ? (2 * c->sms) / bands : 1;
+                a.seg = (nstrips + per_col - 1) / per_col;
+                if (a.seg < 4 * T) a.seg = 4 * T;
+            }
+            if ((nstrips + a.seg - 1) / a.seg > 65535) a.seg = (nstrips + 65534) / 65535;
             a.sd_in = mx->sd[l & 1];
             a.sd_out = mx->sd[(l + 1) & 1];
             a.rt_in = rt[l & 1];
@@ -1120,8 +1144,8 @@ int mixed_ppcg_ur_inner(Chunk *c) {
     Mixed *mx = mixed_of(c);
     int rc;
 #define TL_PP_UR(PC)                                                                                       \
-    BodyPpUr<PC>{c->diag, c->p, c->w, c->mi, c->ky, c->cp, c->bfp, c->u, c->r, mx->sd[0], mx->rtemp,      \
-                 mx->utemp, c->pitch, c->pitch, 0.0, 0.0}
+    BodyPpUr<PC>{c->p, c->w, c->u, c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->sd[0], mx->rtemp, mx->utemp, \
+                 c->pitch, c->pitch, 0.0, 0.f}
     if (c->cfg.precond == TL_PREC_JAC_BLOCK) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_BLOCK), kInNone, true);
     else if (c->cfg.precond == TL_PREC_JAC_DIAG) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_DIAG), kInNone, true);
     else rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_NONE), kInNone, true);

@@ -88,7 +88,7 @@ def test_fused_inner_steps_are_bitwise_equal(precond):
                            tl_use_ppcg=True, tl_ppcg_inner_steps=10, tl_ch_cg_presteps=10,
                            tl_ch_cg_epslim=1.0e10, tl_precision="mixed")
     runs = {}
-    for steps, seg in [(1, 32), (2, 32), (3, 4), (4, 4), (4, 1), (2, 7)]:
+    for steps, seg in [(1, 32), (2, 32), (3, 4), (4, 4), (4, 1), (2, 7), (4, 0)]:
         cfg = tl.parse_deck(deck)
         with tl.Chunk(cfg) as ch:
             ch.set_inner_fusion(steps, seg)
@@ -105,6 +105,6 @@ def test_fused_inner_steps_are_bitwise_equal(precond):
 def test_inner_fusion_rejects_bad_settings():
     cfg = tl.parse_deck(decks.make_deck(x_cells=32, y_cells=32, end_step=1))
     with tl.Chunk(cfg) as ch:
-        for bad in [(0, 32), (5, 32), (2, 0)]:
+        for bad in [(0, 32), (5, 32), (2, -1)]:
             with pytest.raises(tl.TeaLeafError):
                 ch.set_inner_fusion(*bad)
