@@ -184,9 +184,12 @@ int tl_profile_reset(tl_chunk_t *ch);
 /* mixed-precision PPCG: run `steps` (1..4) FP32 inner steps per pass over
  * HBM (temporal blocking; 1 = one kernel per inner step), each CTA taking
  * `seg_strips` 4-row strips of a column band (0: chosen from the grid size,
- * one wave of CTAs).  Results are bitwise the same for every setting; only
- * the speed changes.  Default 4 and 0. */
-int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips);
+ * one wave of CTAs).  The inner steps give the same bits for every setting.
+ * fold_rrn != 0 lets the last fused pass also sum the outer (r - r_store).z,
+ * saving a pass over r, r_store and z; that sum then runs in the fused
+ * grid's order, so solves with different settings agree to round-off rather
+ * than bit for bit.  Default 4, 0, 1. */
+int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips, int fold_rrn);
 int tl_profile_read(tl_chunk_t *ch, int idx, const char **name, long long *launches, double *ms);
 /* the process-wide chunk the reference-named entry points act on */
 tl_chunk_t *tl_default_chunk(void);

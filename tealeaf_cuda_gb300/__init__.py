@@ -152,7 +152,7 @@ def load():
     lib.tl_get_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     lib.tl_set_field.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     lib.tl_set_dt.argtypes = [C.c_void_p, C.c_double]
-    lib.tl_set_inner_fusion.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    lib.tl_set_inner_fusion.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
     lib.tl_kernel_launches.restype = C.c_longlong
     lib.tl_kernel_launches.argtypes = [C.c_void_p]
     lib.tl_default_chunk.restype = C.c_void_p
@@ -246,10 +246,11 @@ class Chunk:
     def set_dt(self, dt):
         _check(load().tl_set_dt(self._h, dt), "tl_set_dt")
 
-    def set_inner_fusion(self, steps, seg_strips=0):
-        """FP32 PPCG inner steps per HBM pass (1..4) and strips per CTA
-        segment (0: automatic)"""
-        _check(load().tl_set_inner_fusion(self._h, steps, seg_strips), "tl_set_inner_fusion")
+    def set_inner_fusion(self, steps, seg_strips=0, fold_rrn=True):
+        """FP32 PPCG inner steps per HBM pass (1..4), strips per CTA segment
+        (0: automatic), and whether the last pass also sums PPCG's rrn"""
+        _check(load().tl_set_inner_fusion(self._h, steps, seg_strips, 1 if fold_rrn else 0),
+               "tl_set_inner_fusion")
 
     def timestep(self):
         info = SolveInfo()

@@ -120,6 +120,7 @@ static int chunk_alloc(const tl_config_t *cfg, Chunk **out) {
     c->dt = cfg->dtinit;
     c->inner_fuse = kInnerFuseDefault;
     c->inner_seg = kInnerSegDefault;
+    c->inner_fold_rrn = true;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     c->sms = sms > 0 ? sms : 152;
@@ -518,7 +519,7 @@ int tl_warm_start_features(tl_chunk_t *ch, float *dst) {
     return warm_features(ch->c, dst);
 }
 
-int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips) {
+int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips, int fold_rrn) {
     if (!ch || !ch->c) {
         set_error("tl_set_inner_fusion: no chunk");
         return TL_ERR_STATE;
@@ -528,9 +529,11 @@ int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips) {
         return TL_ERR_ARG;
     }
     Chunk *c = ch->c;
-    if (c->inner_fuse != steps || c->inner_seg != seg_strips) drop_graphs(c);
+    if (c->inner_fuse != steps || c->inner_seg != seg_strips || c->inner_fold_rrn != (fold_rrn != 0))
+        drop_graphs(c);
     c->inner_fuse = steps;
     c->inner_seg = seg_strips;
+    c->inner_fold_rrn = fold_rrn != 0;
     return TL_OK;
 }
 

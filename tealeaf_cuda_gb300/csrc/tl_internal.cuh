@@ -127,6 +127,7 @@ struct Chunk {
     void *mixed;
     int inner_fuse;              // FP32 PPCG inner steps per HBM pass (1: one kernel per step)
     int inner_seg;               // 4-row strips per CTA segment of the fused inner kernel (0: automatic)
+    bool inner_fold_rrn;         // the last fused inner pass also sums PPCG's rrn
     int sms;                     // multiprocessors of the device
     // learned warm start model and buffers (tl_warm.cu)
     void *warm;
@@ -187,7 +188,7 @@ int launch_copy(Chunk *c, double *dst, const double *src, bool fast);
 int launch_ppcg_rrn(Chunk *c, int epi, bool fast);
 int launch_ppcg_zr(Chunk *c, int epi, bool fast);
 int launch_ppcg_store_zr(Chunk *c, int epi, bool fast);  // r_store = r + ppcg_zr
-int launch_ppcg_w_store_zr(Chunk *c, bool fast);         // cg_w + ppcg_store_zr, one pass
+int launch_ppcg_w_store_zr(Chunk *c, bool fast, bool five);  // cg_w + ppcg_store_zr, one pass
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast);
 int launch_jacobi(Chunk *c, int epi, bool fast);
 int launch_finalise(Chunk *c);
@@ -218,7 +219,9 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
 int mixed_ppcg_prepare(Chunk *c);  // FP32 operator + preconditioner copies
 int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
-int mixed_ppcg_ur_inner(Chunk *c); // the outer u/r update fused with the inner start, then the steps
+// the outer u/r update fused with the inner start, then the steps; *did_rrn
+// tells whether the last pass also summed (r - r_store).z (kEpiPpcgRrn)
+int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn);
 void drop_graphs(Chunk *c);        // after a change that captured graphs depend on
 constexpr int kInnerFuseDefault = 4;
 constexpr int kInnerSegDefault = 0;

@@ -209,7 +209,10 @@ __device__ __forceinline__ double diag_at(const double *__restrict__ kx,
 
 // A x on the m rows of a strip (tea_leaf_common.cuknl:28-34).  xc receives
 // the centre values.  Rows beyond m are neither read nor written.
-template <class X>
+// FIVE: the same operator as one product and four fused subtractions
+// (5 FP64 instructions instead of 6; other rounding, so only for callers
+// that do not need the reference's bits)
+template <class X, bool FIVE = false>
 __device__ __forceinline__ void strip_apply(const double *__restrict__ kx,
                                             const double *__restrict__ ky,
                                             const double *__restrict__ dg, int pitch,
@@ -230,9 +233,17 @@ __device__ __forceinline__ void strip_apply(const double *__restrict__ kx,
             const double kxc = kx[i], kxe = kx[i + 1];
             const double xw = x(i - 1), xe = x(i + 1);
             const double diag = dg[i];
-            const double a = fma(kyr[k + 1], xr[k + 2], kyr[k] * xr[k]);
-            const double b = fma(kxe, xe, kxc * xw);
-            ax[k] = fma(diag, xr[k + 1], -a) - b;
+            if (FIVE) {
+                double v = diag * xr[k + 1];
+                v = fma(-kyr[k + 1], xr[k + 2], v);
+                v = fma(-kyr[k], xr[k], v);
+                v = fma(-kxe, xe, v);
+                ax[k] = fma(-kxc, xw, v);
+            } else {
+                const double a = fma(kyr[k + 1], xr[k + 2], kyr[k] * xr[k]);
+                const double b = fma(kxe, xe, kxc * xw);
+                ax[k] = fma(diag, xr[k + 1], -a) - b;
+            }
             xc[k] = xr[k + 1];
         }
     }
@@ -649,8 +660,10 @@ struct BodyCopy {
     }
 };
 
+template <bool FIVE>
 struct BodyCgWStoreZr {  // BodyCgW and BodyStoreZr in one pass: w = A p, r_store = r;
                          // sums p.w and r.z, each in its own kernel's order
+                         // (FIVE: the 5-instruction operator, mixed precision only)
     const double *dg;
     const double *p, *kx, *ky, *r, *z;
     double *w, *r_store;
@@ -658,7 +671,7 @@ struct BodyCgWStoreZr {  // BodyCgW and BodyStoreZr in one pass: w = A p, r_stor
     __device__ void setup() {}
     __device__ void operator()(int64_t base, int m, double (&acc)[2]) const {
         double xc[4], ax[4];
-        strip_apply(kx, ky, dg, pitch, base, m, LoadX{p}, xc, ax);
+        strip_apply<LoadX, FIVE>(kx, ky, dg, pitch, base, m, LoadX{p}, xc, ax);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
@@ -1090,8 +1103,12 @@ int launch_ppcg_zr(Chunk *c, int epi, bool fast) {
     return run<1>(c, "ppcg_zr", b, epi, fast);
 }
 
-int launch_ppcg_w_store_zr(Chunk *c, bool fast) {
-    BodyCgWStoreZr b{c->diag, c->p, c->kx, c->ky, c->r, c->z, c->w, c->r_store, c->pitch};
+int launch_ppcg_w_store_zr(Chunk *c, bool fast, bool five) {
+    if (five) {
+        BodyCgWStoreZr<true> b{c->diag, c->p, c->kx, c->ky, c->r, c->z, c->w, c->r_store, c->pitch};
+        return run<2>(c, "ppcg_w_zr", b, kEpiPwZr, fast);
+    }
+    BodyCgWStoreZr<false> b{c->diag, c->p, c->kx, c->ky, c->r, c->z, c->w, c->r_store, c->pitch};
     return run<2>(c, "ppcg_w_zr", b, kEpiPwZr, fast);
 }
 

@@ -35,6 +35,7 @@ struct Mixed {
     float *kx, *ky, *mi, *d, *r, *p, *w, *z;
     float *sd[2], *rtemp, *utemp, *cp, *bfp;   // PPCG inner steps
     float *rtemp2;                             // second rtemp of the fused inner passes
+    double *fpartials;                         // one per CTA of a fused inner pass
     double *partials;            // one per CTA of the vectorised kernels
     unsigned int *counter;
     int vtiles_x, vtiles;        // tiles of the vectorised kernels
@@ -576,7 +577,56 @@ struct PpFusedArgs {
     const double *alphas, *betas;
     int step0;                      // inner step of level 1 (1-based)
     double *z64;                    // LAST: z = utemp in FP64
+    // LAST with rrn: also sum (r - r_store).z, the PPCG outer rrn
+    // (tea_leaf_ppcg.cuknl:279-297), and run its scalar update
+    int rrn;
+    const double *r64, *rs64;
+    double *partials;
+    unsigned int *counter;
 };
+
+// CTA + grid sum of the fused pass's rrn (deterministic: warps, then CTAs,
+// in index order); the last CTA updates the PPCG scalars as the FP64
+// path's ppcg_rrn epilogue does: rrn, beta = rrn / rro, error = rro = rrn.
+// Every thread of the CTA calls it.
+__device__ void fused_rrn_reduce(double acc, double *partials, unsigned int *counter, DevScalars *sc) {
+    constexpr int NW = kFusedThreads / 32;
+    __shared__ double sh[NW];
+    __shared__ int is_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) sh[warp] = acc;
+    __syncthreads();
+    const unsigned nb = gridDim.x * gridDim.y, b = blockIdx.y * gridDim.x + blockIdx.x;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < NW; ++w) t += sh[w];
+        partials[b] = t;
+        __threadfence();
+        is_last = atomicAdd(counter, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double t = 0.0;
+    for (unsigned i = threadIdx.x; i < nb; i += blockDim.x) t += __ldcg(&partials[i]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+    __syncthreads();
+    if (lane == 0) sh[warp] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < NW; ++w) tot += sh[w];
+        sc->rrn = tot;
+        sc->beta = tot / sc->rro;
+        sc->error = tot;
+        sc->rro = tot;
+        __threadfence();
+        *counter = 0u;
+    }
+}
 
 // coefficient arrays staged per strip: Kx, Ky, then cp, bfp (block) or Mi (diag),
 // packed per cell as one float4 {Kx, Ky, cp | Mi, bfp}
@@ -595,7 +645,7 @@ __host__ __device__ constexpr size_t fused_smem() {
 }
 
 template <int T, int PC, bool LAST>
-__global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, const DevScalars *__restrict__ sc) {
+__global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, DevScalars *sc) {
     if (*(volatile const int *)&sc->done) return;
     constexpr int NT = kFusedThreads;
     constexpr int SR = kFusedRow;  // shared-memory row stride
@@ -654,6 +704,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
     };
     auto slot_of = [](int q) { return (q + 8 * R) % R; };  // q >= -2T >= -8
     load(sb - T);
+    double racc = 0.0;  // LAST with rrn: this thread's (r - r_store).z
     __syncthreads();
     for (int s = sb - T; s < se + T; ++s) {
         float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
@@ -743,7 +794,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
                     if (k < m) {
                         const int row = 4 * q + k;
                         if (LAST) {
-                            a.z64[(int64_t)cbase + (int64_t)(row + a.h) * a.pitch64] = (double)oU[k];
+                            const int64_t i64 = (int64_t)cbase + (int64_t)(row + a.h) * a.pitch64;
+                            const double zv = (double)oU[k];
+                            a.z64[i64] = zv;
+                            if (a.rrn) racc = fma(a.r64[i64] - a.rs64[i64], zv, racc);
                         } else {
                             const int i = cbase + (row + a.h) * a.pitch;
                             a.sd_out[i] = oS[k];
@@ -756,6 +810,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, co
         }
         __syncthreads();
     }
+    if (LAST && a.rrn) fused_rrn_reduce(racc, a.partials, a.counter, sc);
 }
 
 // FP32 copies of the preconditioner: Mi = 1/diag, block cp, and bfp with
@@ -918,6 +973,13 @@ int mixed_alloc(Chunk *c) {
     TL_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * (size_t)mx->vtiles + 256, c->stream));
     mx->counter = (unsigned int *)p;
     mx->partials = (double *)((char *)p + 256);
+    // the most CTAs a fused pass can have: the narrowest band, one strip per segment
+    const size_t fcta = (size_t)((c->nx + kFusedThreads - 2 * kFusedMax - 1) / (kFusedThreads - 2 * kFusedMax)) *
+                        (size_t)((c->ny + 3) / 4);
+    e = cudaMalloc(&p, sizeof(double) * fcta);
+    if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");
+    mx->allocs.push_back(p);
+    mx->fpartials = (double *)p;
     return TL_OK;
 }
 
@@ -991,7 +1053,7 @@ int mixed_ppcg_prepare(Chunk *c) {
 }
 
 template <int T, int PC, bool LAST>
-void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, const DevScalars *sc) {
+void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, DevScalars *sc) {
     constexpr size_t bytes = fused_smem<T, PC>();
     static bool configured = false;  // the attribute belongs to the kernel: set once
     if (!configured) {
@@ -1003,13 +1065,13 @@ void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, const DevSca
 }
 
 template <int T, int PC>
-void launch_fused(dim3 grid, cudaStream_t s, const PpFusedArgs &a, bool last, const DevScalars *sc) {
+void launch_fused(dim3 grid, cudaStream_t s, const PpFusedArgs &a, bool last, DevScalars *sc) {
     if (last) launch_fused1<T, PC, true>(grid, s, a, sc);
     else launch_fused1<T, PC, false>(grid, s, a, sc);
 }
 
 template <int T>
-void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bool last, const DevScalars *sc) {
+void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bool last, DevScalars *sc) {
     if (pc == TL_PREC_JAC_BLOCK) launch_fused<T, TL_PREC_JAC_BLOCK>(grid, s, a, last, sc);
     else if (pc == TL_PREC_JAC_DIAG) launch_fused<T, TL_PREC_JAC_DIAG>(grid, s, a, last, sc);
     else launch_fused<T, TL_PREC_NONE>(grid, s, a, last, sc);
@@ -1022,8 +1084,11 @@ void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bo
 namespace {
 
 // the inner steps proper, from sd[0], rtemp, utemp to z (FP64)
-int inner_steps(Chunk *c) {
+// rrn: the last fused pass also sums (r - r_store).z and updates the PPCG
+// scalars (*did_rrn reports whether it did: only fused passes can)
+int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
     Mixed *mx = mixed_of(c);
+    *did_rrn = false;
     const int inner = c->cfg.ppcg_inner_steps;
     const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
     const unsigned grid = (unsigned)mx->vtiles;
@@ -1070,6 +1135,11 @@ int inner_steps(Chunk *c) {
             a.betas = c->ch_betas;
             a.step0 = done + 1;
             a.z64 = c->z;
+            a.rrn = (rrn && last) ? 1 : 0;
+            a.r64 = c->r;
+            a.rs64 = c->r_store;
+            a.partials = mx->fpartials;
+            a.counter = mx->counter;
             const dim3 fg((unsigned)((c->nx + a.band - 1) / a.band), (unsigned)((nstrips + a.seg - 1) / a.seg));
             rc = launch_v(c, "mixed_pp_fused", [&] {
                 switch (T) {
@@ -1082,6 +1152,7 @@ int inner_steps(Chunk *c) {
             if (rc) return rc;
             done += T;
         }
+        *did_rrn = rrn;
         return TL_OK;
     }
     for (int st = 1; st <= inner; ++st) {
@@ -1136,10 +1207,11 @@ int mixed_ppcg_inner(Chunk *c) {
                                                                 mx->utemp, c->sc);
          })))
         return rc;
-    return inner_steps(c);
+    bool did_rrn;
+    return inner_steps(c, false, &did_rrn);
 }
 
-int mixed_ppcg_ur_inner(Chunk *c) {
+int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn) {
     if (!inner_ready(c)) return TL_ERR_STATE;
     Mixed *mx = mixed_of(c);
     int rc;
@@ -1151,7 +1223,7 @@ int mixed_ppcg_ur_inner(Chunk *c) {
     else rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_NONE), kInNone, true);
 #undef TL_PP_UR
     if (rc) return rc;
-    return inner_steps(c);
+    return inner_steps(c, c->inner_fold_rrn, did_rrn);
 }
 
 void mixed_free(Chunk *c) {

@@ -73,14 +73,16 @@ int body_cg(Chunk *c) {
 
 int body_ppcg(Chunk *c) {
     int rc;
-    if ((rc = launch_ppcg_w_store_zr(c, true))) return rc;
-    if (c->cfg.precision == TL_PRECISION_MIXED) {
-        if ((rc = mixed_ppcg_ur_inner(c))) return rc;
+    const bool mixed = c->cfg.precision == TL_PRECISION_MIXED;
+    if ((rc = launch_ppcg_w_store_zr(c, true, mixed))) return rc;
+    bool did_rrn = false;
+    if (mixed) {
+        if ((rc = mixed_ppcg_ur_inner(c, &did_rrn))) return rc;
     } else {
         if ((rc = launch_cg_ur(c, 0.0, kEpiNone, true))) return rc;
         if ((rc = ppcg_inner_steps(c, true))) return rc;
     }
-    if ((rc = launch_ppcg_rrn(c, kEpiPpcgRrn, true))) return rc;
+    if (!did_rrn && (rc = launch_ppcg_rrn(c, kEpiPpcgRrn, true))) return rc;
     if ((rc = launch_ppcg_p(c, 0.0, kEpiFinishNoSwitch, true))) return rc;
     return halo(c, TL_FIELD_P, 1);
 }

@@ -79,32 +79,52 @@ def test_mixed_ppcg_matches_fp64(precond):
         assert err < 1e-9
 
 
-@pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
-def test_fused_inner_steps_are_bitwise_equal(precond):
-    """The temporally blocked inner steps (2-4 per pass, any segment height)
-    give the bits of one kernel per inner step; 600 x 150 cells make several
-    column bands, a partial last strip and many row segments."""
+def _fusion_runs(precond, settings):
     deck = decks.make_deck(x_cells=600, y_cells=150, end_step=2, tl_preconditioner_type=precond, tl_use_cg=False,
                            tl_use_ppcg=True, tl_ppcg_inner_steps=10, tl_ch_cg_presteps=10,
                            tl_ch_cg_epslim=1.0e10, tl_precision="mixed")
     runs = {}
-    for steps, seg in [(1, 32), (2, 32), (3, 4), (4, 4), (4, 1), (2, 7), (4, 0)]:
+    for key in settings:
         cfg = tl.parse_deck(deck)
         with tl.Chunk(cfg) as ch:
-            ch.set_inner_fusion(steps, seg)
+            ch.set_inner_fusion(*key)
             ch.start()
             its = [ch.timestep()["iterations"] for _ in range(2)]
-            runs[(steps, seg)] = (its, ch.interior("u").copy(), ch.field_summary())
-    its0, u0, fs0 = runs[(1, 32)]
+            runs[key] = (its, ch.interior("u").copy(), ch.field_summary())
+    return runs
+
+
+@pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
+def test_fused_inner_steps_are_bitwise_equal(precond):
+    """The temporally blocked inner steps (2-4 per pass, any segment height)
+    give the bits of one kernel per inner step; 600 x 150 cells make several
+    column bands, a partial last strip and many row segments.  (The outer
+    rrn sum stays in its own kernel here: fold_rrn off.)"""
+    runs = _fusion_runs(precond, [(1, 32, False), (2, 32, False), (3, 4, False), (4, 4, False),
+                                  (4, 1, False), (2, 7, False), (4, 0, False)])
+    its0, u0, fs0 = runs[(1, 32, False)]
     for key, (its, u, fs) in runs.items():
         assert its == its0, key
         assert np.array_equal(u, u0), key
         assert fs == fs0, key
 
 
+@pytest.mark.parametrize("precond", ["jac_diag", "jac_block"])
+def test_folded_rrn_matches_to_round_off(precond):
+    """With the outer (r - r_store).z summed inside the last fused pass the
+    sum runs in another order: the solve must agree to round-off."""
+    runs = _fusion_runs(precond, [(1, 32, False), (4, 0, True), (3, 5, True), (2, 1, True)])
+    its0, u0, fs0 = runs[(1, 32, False)]
+    for key, (its, u, fs) in runs.items():
+        assert all(abs(a - b) <= 1 for a, b in zip(its, its0)), key
+        assert np.max(np.abs(u - u0)) / np.max(np.abs(u0)) < 1e-12, key
+        for a, b in zip(fs, fs0):
+            assert a == pytest.approx(b, rel=1e-12), key
+
+
 def test_inner_fusion_rejects_bad_settings():
     cfg = tl.parse_deck(decks.make_deck(x_cells=32, y_cells=32, end_step=1))
     with tl.Chunk(cfg) as ch:
-        for bad in [(0, 32), (5, 32), (2, -1)]:
+        for bad in [(0, 32, 1), (5, 32, 1), (2, -1, 1)]:
             with pytest.raises(tl.TeaLeafError):
                 ch.set_inner_fusion(*bad)
