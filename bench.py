@@ -111,6 +111,12 @@ def bytes_per_cell(kernel, precond):
         # 1/b of the strip solve); write sd', rtemp, utemp (an inner step
         # before the last)
         return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
+    if kernel == "mixed_ur":
+        # read d, p, r, w + the preconditioner (Mi; or Ky, cp, bfp); write d, r, z
+        return {"none": 28, "jac_diag": 32, "jac_block": 40}[precond]
+    if kernel == "mixed_init":
+        # read r (FP64) + the preconditioner; write r, z, p, d
+        return {"none": 24, "jac_diag": 28, "jac_block": 36}[precond]
     if kernel == "mixed_pp_ur":
         # read u, p, w, r (FP64) + the FP32 preconditioner (Mi; or Ky, cp,
         # bfp); write u, r (FP64) and rtemp, sd, utemp (FP32)

@@ -188,7 +188,8 @@ int tl_profile_reset(tl_chunk_t *ch);
  * fold_rrn != 0 lets the last fused pass also sum the outer (r - r_store).z,
  * saving a pass over r, r_store and z; that sum then runs in the fused
  * grid's order, so solves with different settings agree to round-off rather
- * than bit for bit.  Default 4, 0, 1. */
+ * than bit for bit (and on GB300 the fold is slower: it adds FP64 work to
+ * an issue-bound pass).  Default 4, 0, 0. */
 int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips, int fold_rrn);
 int tl_profile_read(tl_chunk_t *ch, int idx, const char **name, long long *launches, double *ms);
 /* the process-wide chunk the reference-named entry points act on */

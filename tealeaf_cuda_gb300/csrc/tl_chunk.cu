@@ -120,7 +120,7 @@ static int chunk_alloc(const tl_config_t *cfg, Chunk **out) {
     c->dt = cfg->dtinit;
     c->inner_fuse = kInnerFuseDefault;
     c->inner_seg = kInnerSegDefault;
-    c->inner_fold_rrn = true;
+    c->inner_fold_rrn = false;  // measured slower on GB300: its FP64 work lands in an issue-bound pass
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
     c->sms = sms > 0 ? sms : 152;

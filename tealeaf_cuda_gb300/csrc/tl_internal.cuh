@@ -35,7 +35,11 @@ struct DevScalars {
     double theta;                  // Chebyshev / PPCG centre of the spectrum
     // inner FP32 Krylov solve of the mixed form (its scalars stay FP64)
     double in_rro, in_pw, in_rrn, in_alpha, in_beta, in_target;
+    // FP32 CG presteps of mixed PPCG: where the inner epilogues record the
+    // Lanczos coefficients (the cg_alphas / cg_betas of the FP64 path)
+    double *lanczos_a, *lanczos_b;
     int in_n, in_max;
+    int prestep;                   // 1: the inner epilogues act as the CG phase's
     int n;                         // current iteration (1-based)
     int max_iters;
     int done;                      // 0 running, 1 converged, 2 max_iters, 3 switch, 4 breakdown
@@ -215,9 +219,14 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info);       // tl_solve.cu
 // device sets DevScalars::done; *done_out receives it (tl_solve.cu)
 int run_phase(Chunk *c, int (*body)(Chunk *), int iters, int phase, int *done_out);
 constexpr int kPhaseMixedInner = 4;
+constexpr int kPhaseMixedPre = 5;
 int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info); // tl_mixed.cu
 void mixed_free(Chunk *c);
 int mixed_ppcg_prepare(Chunk *c);  // FP32 operator + preconditioner copies
+// the CG presteps of the first PPCG solve in FP32 (FP64 scalars and Lanczos
+// coefficients): runs until the switch test, then u += d and r = u0 - A u in
+// FP64; *done_out gets the device's exit code (kSwitch when it switched)
+int mixed_ppcg_presteps(Chunk *c, int *done_out);
 int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
 // the outer u/r update fused with the inner start, then the steps; *did_rrn
 // tells whether the last pass also summed (r - r_store).z (kEpiPpcgRrn)

@@ -91,6 +91,7 @@ __device__ void inner_epilogue(DevScalars *s, int epi, double tot) {
     case kInW:
         s->in_pw = tot;
         s->in_alpha = s->in_rro / s->in_pw;
+        if (s->prestep) s->lanczos_a[s->n] = s->in_alpha;  // cg_alphas (tea_leaf_cg.f90)
         break;
     case kInUr: {
         s->in_rrn = tot;
@@ -98,6 +99,29 @@ __device__ void inner_epilogue(DevScalars *s, int epi, double tot) {
         s->in_rro = s->in_rrn;
         s->in_n += 1;
         const double e = sqrt(fabs(tot));
+        if (s->prestep) {
+            // the CG phase of tea_solve.f90:400-417 and its switch test
+            // (:157-171), as the FP64 path's finish_iteration
+            s->lanczos_b[s->n] = s->in_beta;
+            s->error = e;
+            if (fabs(e) < s->eps * s->initial_residual) {
+                s->done = kConverged;
+                s->n_exit = s->n;
+            } else if (isnan(e)) {
+                s->done = kBreakdown;
+                s->n_exit = s->n;
+            } else {
+                s->old_error = e;
+                s->n += 1;
+                if (s->n > s->max_iters) {
+                    s->done = kMaxIters;
+                    s->n_exit = s->n;
+                } else if ((!s->first && s->n > 1) || (fabs(s->old_error) <= s->epslim && s->n >= s->presteps)) {
+                    s->done = kSwitch;
+                }
+            }
+            break;
+        }
         if (isnan(e)) s->done = kBreakdown;
         else if (e < s->in_target || s->in_n >= s->in_max) s->done = kConverged;
         break;
@@ -294,16 +318,23 @@ __global__ void __launch_bounds__(kBlockThreads) k_v_w(GeoV g, const float *__re
     reduce_v(acc, partials, counter, sc, kInW);
 }
 
-// d += alpha p; r -= alpha w; z = Mi r (DIAG) ; sum r.z
-template <bool DIAG>
+// d += alpha p; r -= alpha w; z = M^-1 r; sum r.z.  PC: TL_PREC_NONE (z = r,
+// not stored), TL_PREC_JAC_DIAG (z = Mi r) or TL_PREC_JAC_BLOCK (the 4-row
+// strip solve of k_pp_step on the warp's two strips; ky, cp and bfp with
+// 1/diag in each strip's first row)
+template <int PC>
 __global__ void __launch_bounds__(kBlockThreads) k_v_ur(GeoV g, float *__restrict__ d,
                                                         float *__restrict__ r,
                                                         float *__restrict__ z,
                                                         const float *__restrict__ p,
                                                         const float *__restrict__ w,
                                                         const float *__restrict__ mi,
+                                                        const float *__restrict__ ky,
+                                                        const float *__restrict__ cp,
+                                                        const float *__restrict__ bfp,
                                                         double *partials, unsigned int *counter,
                                                         DevScalars *sc) {
+    constexpr bool DIAG = PC == TL_PREC_JAC_DIAG;
     if (*(volatile const int *)&sc->done) return;
     const float alpha = (float)sc->in_alpha;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -311,7 +342,62 @@ __global__ void __launch_bounds__(kBlockThreads) k_v_ur(GeoV g, float *__restric
     const int j0 = (blockIdx.x / g.tiles_x) * kVTileRows + warp * kVRows;
     const int nv = min(4, g.nx - c);
     CSum acc = {0.f, 0.f};
-    if (j0 < g.ny && nv > 0) {
+    if (PC == TL_PREC_JAC_BLOCK && j0 < g.ny && nv > 0) {
+        const int64_t P = g.pitch;
+#pragma unroll
+        for (int s0 = 0; s0 < kVRows; s0 += 4) {
+            if (j0 + s0 >= g.ny) break;
+            const int m = min(4, g.ny - (j0 + s0));
+            const int64_t i0 = (int64_t)(c + g.h) + (int64_t)(j0 + s0 + g.h) * P;
+            float4 rv[4], zv[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k >= m) break;
+                const int64_t i = i0 + (int64_t)k * P;
+                const float4 pv = ld4(p, i), wv = ld4(w, i), rv0 = ld4(r, i), dv0 = ld4(d, i);
+                float4 dv;
+                dv.x = fmaf(alpha, pv.x, dv0.x);
+                dv.y = fmaf(alpha, pv.y, dv0.y);
+                dv.z = fmaf(alpha, pv.z, dv0.z);
+                dv.w = fmaf(alpha, pv.w, dv0.w);
+                rv[k].x = fmaf(-alpha, wv.x, rv0.x);
+                rv[k].y = fmaf(-alpha, wv.y, rv0.y);
+                rv[k].z = fmaf(-alpha, wv.z, rv0.z);
+                rv[k].w = fmaf(-alpha, wv.w, rv0.w);
+                st4(d, i, dv, nv);
+                st4(r, i, rv[k], nv);
+                // Thomas forward sweep: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k
+                const float4 bf = ld4(bfp, i);
+                if (k == 0) {
+                    zv[0] = make_float4(rv[0].x * bf.x, rv[0].y * bf.y, rv[0].z * bf.z, rv[0].w * bf.w);
+                } else {
+                    const float4 kyk = ld4(ky, i);
+                    zv[k].x = fmaf(kyk.x, zv[k - 1].x, rv[k].x) * bf.x;
+                    zv[k].y = fmaf(kyk.y, zv[k - 1].y, rv[k].y) * bf.y;
+                    zv[k].z = fmaf(kyk.z, zv[k - 1].z, rv[k].z) * bf.z;
+                    zv[k].w = fmaf(kyk.w, zv[k - 1].w, rv[k].w) * bf.w;
+                }
+            }
+#pragma unroll
+            for (int k = 2; k >= 0; --k) {
+                if (k >= m - 1) continue;
+                const float4 cv = ld4(cp, i0 + (int64_t)k * P);
+                zv[k].x = fmaf(-cv.x, zv[k + 1].x, zv[k].x);
+                zv[k].y = fmaf(-cv.y, zv[k + 1].y, zv[k].y);
+                zv[k].z = fmaf(-cv.z, zv[k + 1].z, zv[k].z);
+                zv[k].w = fmaf(-cv.w, zv[k + 1].w, zv[k].w);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (k >= m) break;
+                st4(z, i0 + (int64_t)k * P, zv[k], nv);
+                csum_add(acc, rv[k].x * zv[k].x);
+                if (nv > 1) csum_add(acc, rv[k].y * zv[k].y);
+                if (nv > 2) csum_add(acc, rv[k].z * zv[k].z);
+                if (nv > 3) csum_add(acc, rv[k].w * zv[k].w);
+            }
+        }
+    } else if (j0 < g.ny && nv > 0) {
         const int64_t P = g.pitch;
         int64_t i = (int64_t)(c + g.h) + (int64_t)(j0 + g.h) * P;
 #pragma unroll
@@ -852,25 +938,39 @@ struct BodyConvert {
     }
 };
 
-template <bool DIAG>
+template <int PC>
 struct BodyInnerInit {  // r = (float) r64; z = M^-1 r; p = z; d = 0; sum r.z
     const double *r64;
-    const float *mi;
+    const float *mi, *ky, *cp, *bfp;
     float *r, *z, *p, *d;
     int pitch32, pitch64;
     __device__ void setup(DevScalars *) {}
     __device__ void operator()(int64_t b32, int64_t b64, int m, CSum &acc) const {
+        float rv[4], zv[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t j = b32 + (int64_t)k * pitch32;
-                const float rv = (float)r64[b64 + (int64_t)k * pitch64];
-                const float zv = DIAG ? rv * mi[j] : rv;
-                r[j] = rv;
-                z[j] = zv;
-                p[j] = zv;
+                rv[k] = (float)r64[b64 + (int64_t)k * pitch64];
+                if (PC == TL_PREC_JAC_BLOCK)
+                    zv[k] = k == 0 ? rv[0] * bfp[j] : fmaf(ky[j], zv[k - 1], rv[k]) * bfp[j];
+                else
+                    zv[k] = PC == TL_PREC_JAC_DIAG ? rv[k] * mi[j] : rv[k];
+            }
+        if (PC == TL_PREC_JAC_BLOCK) {
+#pragma unroll
+            for (int k = 2; k >= 0; --k)
+                if (k < m - 1) zv[k] = fmaf(-cp[b32 + (int64_t)k * pitch32], zv[k + 1], zv[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t j = b32 + (int64_t)k * pitch32;
+                r[j] = rv[k];
+                z[j] = zv[k];
+                p[j] = zv[k];
                 d[j] = 0.f;
-                csum_add(acc, rv * zv);
+                csum_add(acc, rv[k] * zv[k]);
             }
     }
 };
@@ -1010,9 +1110,10 @@ int launch_v(Chunk *c, const char *name, F &&launch) {
     return TL_OK;
 }
 
-int inner_body(Chunk *c) {
+template <int PC>
+int inner_body_pc(Chunk *c) {
     Mixed *mx = mixed_of(c);
-    const bool diag = c->cfg.precond != TL_PREC_NONE;
+    const bool diag = PC != TL_PREC_NONE;
     const GeoV g{c->nx, c->ny, c->h, c->pitch, mx->vtiles_x, mx->vtiles};
     const unsigned grid = (unsigned)mx->vtiles;
     cudaStream_t s = c->stream;
@@ -1023,17 +1124,28 @@ int inner_body(Chunk *c) {
          })))
         return rc;
     if ((rc = launch_v(c, "mixed_ur", [&] {
-             if (diag)
-                 k_v_ur<true><<<grid, kBlockThreads, 0, s>>>(g, mx->d, mx->r, mx->z, mx->p, mx->w,
-                                                             mx->mi, mx->partials, mx->counter, c->sc);
-             else
-                 k_v_ur<false><<<grid, kBlockThreads, 0, s>>>(g, mx->d, mx->r, mx->z, mx->p, mx->w,
-                                                              mx->mi, mx->partials, mx->counter, c->sc);
+             k_v_ur<PC><<<grid, kBlockThreads, 0, s>>>(g, mx->d, mx->r, mx->z, mx->p, mx->w, mx->mi, mx->ky,
+                                                       mx->cp, mx->bfp, mx->partials, mx->counter, c->sc);
          })))
         return rc;
     return launch_v(c, "mixed_p", [&] {
         k_v_p<<<grid, kBlockThreads, 0, s>>>(g, mx->p, diag ? mx->z : mx->r, c->sc);
     });
+}
+
+// the inner CG iteration of the mixed CG solve (none or jac_diag)
+int inner_body(Chunk *c) {
+    return c->cfg.precond == TL_PREC_JAC_DIAG ? inner_body_pc<TL_PREC_JAC_DIAG>(c)
+                                              : inner_body_pc<TL_PREC_NONE>(c);
+}
+
+// the FP32 CG presteps of mixed PPCG (any preconditioner)
+int prestep_body(Chunk *c) {
+    switch (c->cfg.precond) {
+    case TL_PREC_JAC_BLOCK: return inner_body_pc<TL_PREC_JAC_BLOCK>(c);
+    case TL_PREC_JAC_DIAG: return inner_body_pc<TL_PREC_JAC_DIAG>(c);
+    default: return inner_body_pc<TL_PREC_NONE>(c);
+    }
 }
 
 }  // namespace
@@ -1226,6 +1338,44 @@ int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn) {
     return inner_steps(c, c->inner_fold_rrn, did_rrn);
 }
 
+int mixed_ppcg_presteps(Chunk *c, int *done_out) {
+    Mixed *mx = mixed_of(c);
+    if (!mx) {
+        set_error("mixed PPCG presteps need a prepared chunk");
+        return TL_ERR_STATE;
+    }
+    int rc;
+    DevScalars &h = *c->sc_host;
+    if ((rc = chunk_sync_scalars(c))) return rc;
+    h.prestep = 1;
+    h.lanczos_a = c->cg_alphas;
+    h.lanczos_b = c->cg_betas;
+    h.in_target = 0.0;
+    if ((rc = chunk_push_scalars(c))) return rc;
+    // r = (float) r, z = M^-1 r, p = z, d = 0, in_rro = r.z
+#define TL_PRE_INIT(PC)                                                                                        \
+    run32(c, "mixed_init", BodyInnerInit<PC>{c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->r, mx->z, mx->p, mx->d, \
+                                              c->pitch, c->pitch},                                             \
+          kInInit, false)
+    if (c->cfg.precond == TL_PREC_JAC_BLOCK) rc = TL_PRE_INIT(TL_PREC_JAC_BLOCK);
+    else if (c->cfg.precond == TL_PREC_JAC_DIAG) rc = TL_PRE_INIT(TL_PREC_JAC_DIAG);
+    else rc = TL_PRE_INIT(TL_PREC_NONE);
+#undef TL_PRE_INIT
+    if (rc) return rc;
+    int done = kRunning;
+    if ((rc = run_phase(c, prestep_body, kItersInner, kPhaseMixedPre, &done))) return rc;
+    // u += d, r = u0 - A u (FP64): the phase after the switch starts from the
+    // true residual
+    BodyUpdateU bu{c->u, mx->d, c->pitch, c->pitch};
+    if ((rc = run32(c, "mixed_update_u", bu, kInNone, false))) return rc;
+    if ((rc = launch_residual(c, kEpiNone))) return rc;
+    if ((rc = chunk_sync_scalars(c))) return rc;
+    h.prestep = 0;
+    if ((rc = chunk_push_scalars(c))) return rc;
+    *done_out = done;
+    return TL_OK;
+}
+
 void mixed_free(Chunk *c) {
     Mixed *mx = mixed_of(c);
     if (!mx) return;
@@ -1291,10 +1441,12 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
         h.in_max = cf.max_iters - inner_total;
         if ((rc = chunk_push_scalars(c))) return rc;
         if (diag) {
-            BodyInnerInit<true> bi{c->r, mx->mi, mx->r, mx->z, mx->p, mx->d, c->pitch, c->pitch};
+            BodyInnerInit<TL_PREC_JAC_DIAG> bi{c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->r, mx->z, mx->p, mx->d,
+                                               c->pitch, c->pitch};
             if ((rc = run32(c, "mixed_init", bi, kInInit, false))) return rc;
         } else {
-            BodyInnerInit<false> bi{c->r, mx->mi, mx->r, mx->z, mx->p, mx->d, c->pitch, c->pitch};
+            BodyInnerInit<TL_PREC_NONE> bi{c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->r, mx->z, mx->p, mx->d,
+                                           c->pitch, c->pitch};
             if ((rc = run32(c, "mixed_init", bi, kInInit, false))) return rc;
         }
         int done = kRunning;

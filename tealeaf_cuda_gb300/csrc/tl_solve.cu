@@ -234,6 +234,10 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info) {
 
     Phase phase = krylov ? kPhaseCg : kPhaseJacobi;
     bool switching = false;
+    // mixed PPCG: the CG presteps of the first solve (which feed the
+    // eigenvalue estimates) run in FP32 with FP64 scalars
+    bool fp32_presteps = use_pp && cf.precision == TL_PRECISION_MIXED && c->first && !cf.reflective_boundary &&
+                         cf.max_iters >= 1;
     if ((use_ch || use_pp) && cf.max_iters >= 1) {
         // the switch test of tea_solve.f90:157-171 at n = 1
         if (fabs(h.old_error) <= cf.ch_cg_epslim && 1 >= cf.ch_cg_presteps) switching = true;
@@ -327,7 +331,19 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info) {
         }
         switch (phase) {
         case kPhaseCg:
-            rc = run_phase(c, body_cg, kItersCg, kPhaseCg, &done);
+            if (fp32_presteps) {
+                fp32_presteps = false;
+                rc = mixed_ppcg_presteps(c, &done);
+                // an FP32 residual below tl_eps is not the FP64 one: let PPCG
+                // confirm it (unless there was nothing to solve)
+                if (!rc && done == kConverged && h.n > 1) {
+                    h.done = kSwitch;
+                    if ((rc = chunk_push_scalars(c))) return rc;
+                    done = kSwitch;
+                }
+            } else {
+                rc = run_phase(c, body_cg, kItersCg, kPhaseCg, &done);
+            }
             break;
         case kPhasePpcg:
             rc = run_phase(c, body_ppcg, kItersPpcg, kPhasePpcg, &done);

@@ -370,6 +370,45 @@ def evaluate(params, seeds, n, steps, precond="jac_diag"):
     return rows
 
 
+def compare_methods(params, seeds, n, steps):
+    """Plain FP64 CG + jac_diag from u = u^n against the headline method
+    (PPCG + block-Jacobi, 10 FP32 inner steps under the FP64 outer solve,
+    learned warm start) on seeded random decks: per timestep the
+    iterations, the solve's wall time and the field summaries."""
+    from . import PREC_JAC_BLOCK, PRECISION_MIXED, SOLVER_PPCG
+    lib = load()
+    rows = []
+    for seed in seeds:
+        deck = random_deck(seed, n, steps)
+        out = {}
+        for name in ("plain", "headline"):
+            cfg = parse_deck(deck)
+            if name == "headline":
+                cfg.solver = SOLVER_PPCG
+                cfg.precond = PREC_JAC_BLOCK
+                cfg.ppcg_inner_steps = 10
+                cfg.precision = PRECISION_MIXED
+                cfg.warm_start = WARM["learned"]
+            recs = []
+            with Chunk(cfg) as ch:
+                ch.start()
+                if name == "headline":
+                    p = np.ascontiguousarray(params, dtype=np.float32)
+                    assert lib.tl_set_warm_start_model(ch._h, C.c_void_p(p.ctypes.data), p.size) == 0
+                for _ in range(steps):
+                    info = ch.timestep()
+                    recs.append((info["iterations"], info["seconds"], ch.field_summary()))
+            out[name] = recs
+        rows.append({"seed": seed,
+                     "plain_iters": [r[0] for r in out["plain"]],
+                     "headline_iters": [r[0] for r in out["headline"]],
+                     "plain_seconds": [r[1] for r in out["plain"]],
+                     "headline_seconds": [r[1] for r in out["headline"]],
+                     "summary_rel_diff": [max(abs(a - b) / abs(b) for a, b in zip(h[2], q[2]))
+                                          for h, q in zip(out["headline"], out["plain"])]})
+    return rows
+
+
 def summarise(rows):
     """totals of evaluate()'s rows"""
     out = {}
@@ -382,10 +421,11 @@ def summarise(rows):
 
 
 def main(argv=None):
-    """python -m tealeaf_cuda_gb300.learned train|evaluate ...
+    """python -m tealeaf_cuda_gb300.learned train|evaluate|compare ...
 
     train:    trajectories of seeded random decks -> model file (+ JSON report)
-    evaluate: plain vs learned start on held-out seeds (JSON report)"""
+    evaluate: plain vs previous-step vs learned start on held-out seeds
+    compare:  plain FP64 CG against the headline method on held-out seeds"""
     import argparse
     import json
     import time
@@ -409,7 +449,25 @@ def main(argv=None):
     e.add_argument("--n", type=int, default=2048)
     e.add_argument("--steps", type=int, default=3)
     e.add_argument("--report", default=None)
+    m = sub.add_parser("compare")
+    m.add_argument("--model", required=True)
+    m.add_argument("--seeds", default="20000-20002")
+    m.add_argument("--n", type=int, default=8192)
+    m.add_argument("--steps", type=int, default=5)
+    m.add_argument("--report", default=None)
     a = ap.parse_args(argv)
+    if a.cmd == "compare":
+        lo, hi = (int(x) for x in a.seeds.split("-"))
+        rows = compare_methods(load_model(a.model), list(range(lo, hi + 1)), a.n, a.steps)
+        tp = sum(sum(r["plain_seconds"]) for r in rows)
+        th = sum(sum(r["headline_seconds"]) for r in rows)
+        rep = {"n": a.n, "steps": a.steps, "seeds": a.seeds, "plain_seconds": tp, "headline_seconds": th,
+               "speedup": tp / th, "max_summary_rel_diff": max(max(r["summary_rel_diff"]) for r in rows),
+               "decks": rows}
+        print(json.dumps({k: v for k, v in rep.items() if k != "decks"}))
+        if a.report:
+            json.dump(rep, open(a.report, "w"), indent=1)
+        return
     if a.cmd == "train":
         t0 = time.time()
         seeds = list(range(a.first_seed, a.first_seed + a.decks))
