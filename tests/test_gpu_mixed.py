@@ -75,8 +75,14 @@ def test_mixed_ppcg_matches_fp64(precond):
             assert b == pytest.approx(a, rel=FS_RTOL), step
         err = np.max(np.abs(umx - u64)) / np.max(np.abs(u64))
         print(f"ppcg {precond} step {step}: outer its fp64 {i64['iterations']} mixed {imx['iterations']}, "
-              f"max|du|/max|u| = {err:.2e}")
+              f"max|du|/max|u| = {err:.2e}, eigenvalues fp64 {i64['eigmin']:.6g} {i64['eigmax']:.6g} "
+              f"mixed {imx['eigmin']:.6g} {imx['eigmax']:.6g}")
         assert err < 1e-9
+        # the first solve's CG presteps run in FP32 there: the same switch
+        # step and the same spectrum estimate from their Lanczos coefficients
+        assert imx["switch_n"] == i64["switch_n"]
+        assert imx["eigmin"] == pytest.approx(i64["eigmin"], rel=1e-3)
+        assert imx["eigmax"] == pytest.approx(i64["eigmax"], rel=1e-3)
 
 
 def _fusion_runs(precond, settings):
