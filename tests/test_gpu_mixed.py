@@ -61,11 +61,13 @@ def test_mixed_reaches_tl_eps_on_the_true_residual():
     assert info["error_ratio"] < 1e-12
 
 
-@pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
-def test_mixed_ppcg_matches_fp64(precond):
+@pytest.mark.parametrize("precond,shape", [("none", (96, 80)), ("jac_diag", (96, 80)), ("jac_block", (96, 80)),
+                                            ("jac_block", (97, 43)), ("jac_diag", (131, 58))])
+def test_mixed_ppcg_matches_fp64(precond, shape):
     """PPCG with its polynomial preconditioner (the 10 inner steps) in FP32:
-    the outer flexible CG stays FP64 and reaches the same answer."""
-    base = dict(x_cells=96, y_cells=80, end_step=3, tl_preconditioner_type=precond, tl_use_cg=False,
+    the outer flexible CG stays FP64 and reaches the same answer (odd sizes:
+    ragged float4 lanes and a partial last block-Jacobi strip)."""
+    base = dict(x_cells=shape[0], y_cells=shape[1], end_step=3, tl_preconditioner_type=precond, tl_use_cg=False,
                 tl_use_ppcg=True, tl_ppcg_inner_steps=10, tl_ch_cg_presteps=10, tl_ch_cg_epslim=1.0e10)
     fp64 = _solve_steps(decks.make_deck(**base), 3)
     mixed = _solve_steps(decks.make_deck(tl_precision="mixed", **base), 3)
