@@ -81,7 +81,6 @@ BYTES_PER_CELL = {
     "finalise": 24,
     "ppcg_p": 24,        # read z, p; write p
     "copy": 16,          # read src; write dst
-    "ppcg_store_zr": 24,  # read r, z; write r_store
     "ppcg_w_zr": 64,     # read p, Kx, Ky, diag, r, z; write w, r_store
     "ppcg_rrn": 24,      # read r, r_store, z
     # mixed precision: FP32 inner iteration (4-byte elements)

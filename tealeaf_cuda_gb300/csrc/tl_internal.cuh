@@ -191,7 +191,6 @@ int launch_ppcg_calc_sd_new(Chunk *c, int step, bool fast);
 int launch_copy(Chunk *c, double *dst, const double *src, bool fast);
 int launch_ppcg_rrn(Chunk *c, int epi, bool fast);
 int launch_ppcg_zr(Chunk *c, int epi, bool fast);
-int launch_ppcg_store_zr(Chunk *c, int epi, bool fast);  // r_store = r + ppcg_zr
 int launch_ppcg_w_store_zr(Chunk *c, bool fast, bool five);  // cg_w + ppcg_store_zr, one pass
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast);
 int launch_jacobi(Chunk *c, int epi, bool fast);

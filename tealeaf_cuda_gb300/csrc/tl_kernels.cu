@@ -685,24 +685,6 @@ struct BodyCgWStoreZr {  // BodyCgW and BodyStoreZr in one pass: w = A p, r_stor
     }
 };
 
-struct BodyStoreZr {  // r_store = r and sum r.z in one pass (tea_leaf_ppcg.cuknl:302-313 + the
-                      // r.z norm); the sum is BodyNorm{r, z}'s, in the same order
-    const double *r, *z;
-    double *r_store;
-    int pitch;
-    __device__ void setup() {}
-    __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k < m) {
-                const int64_t i = base + (int64_t)k * pitch;
-                const double rv = r[i];
-                r_store[i] = rv;
-                acc[0] = fma(rv, z[i], acc[0]);
-            }
-    }
-};
-
 struct BodyPpcgRrn {  // sum (r - r_store).z  (tea_leaf_ppcg.cuknl:279-297)
     const double *r, *r_store, *z;
     int pitch;
@@ -1110,11 +1092,6 @@ int launch_ppcg_w_store_zr(Chunk *c, bool fast, bool five) {
     }
     BodyCgWStoreZr<false> b{c->diag, c->p, c->kx, c->ky, c->r, c->z, c->w, c->r_store, c->pitch};
     return run<2>(c, "ppcg_w_zr", b, kEpiPwZr, fast);
-}
-
-int launch_ppcg_store_zr(Chunk *c, int epi, bool fast) {
-    BodyStoreZr b{c->r, c->z, c->r_store, c->pitch};
-    return run<1>(c, "ppcg_store_zr", b, epi, fast);
 }
 
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast) {
