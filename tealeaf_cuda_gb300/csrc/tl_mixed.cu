@@ -816,6 +816,33 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
             const float *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * 4 * SR + tid;
             const float(&x0)[4] = sdP[t - 1];
             float oS[4], oR[4], oU[4];
+            // the strip's coefficient rows, one float4 each, and the east
+            // neighbours' Kx by shuffle (the last lane reads its neighbour's
+            // row): read once per level by every lane, before the row tests,
+            // so that no single float is read out of the packed rows
+            // (T = 4 has no registers to spare for this: it reads the rows
+            // where it uses them)
+            constexpr bool PRE = T <= 3;
+            float4 c4[4];
+            float kxe4[4], ky_top = 0.f;
+            if constexpr (PRE) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) c4[k] = cf[k * SR];
+                ky_top = cn[0].y;  // the face above the strip's last row
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    kxe4[k] = __shfl_down_sync(0xffffffffu, c4[k].x, 1);
+                    if ((tid & 31) == 31) kxe4[k] = cf[k * SR + 1].x;
+                }
+            }
+            auto row = [&](int k) -> float4 {
+                if constexpr (PRE) return c4[k];
+                else return cf[k * SR];
+            };
+            auto east_kx = [&](int k) -> float {
+                if constexpr (PRE) return kxe4[k];
+                else return cf[k * SR + 1].x;
+            };
             // one inner step on the strip's first mm rows (mm == 4: no row tests)
             auto step = [&](const int mm) {
                 float z[4];
@@ -826,10 +853,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
                         const float c = x0[k];
                         const float n = k < 3 ? x0[k + 1] : cS[0];
                         const float sv = k > 0 ? x0[k - 1] : sdL[t - 1];
-                        const float4 cc = cf[k * SR];
-                        const float kyn = k < 3 ? cf[(k + 1) * SR].y : cn[0].y;
+                        const float4 cc = row(k);
+                        const float kyn = k < 3 ? row(k < 3 ? k + 1 : 3).y : (PRE ? ky_top : cn[0].y);
                         oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, xp[k * SR - 1], xp[k * SR + 1], kyn, cc.y,
-                                                           cf[k * SR + 1].x, cc.x);
+                                                           east_kx(k), cc.x);
                     }
                 }
                 if constexpr (PC == TL_PREC_JAC_BLOCK) {
@@ -838,17 +865,17 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         if (k < mm) {
-                            const float4 cc = cf[k * SR];
+                            const float4 cc = row(k);
                             z[k] = k == 0 ? oR[0] * cc.w : fmaf(cc.y, z[k - 1], oR[k]) * cc.w;
                         }
                     }
 #pragma unroll
                     for (int k = 2; k >= 0; --k)
-                        if (k < mm - 1) z[k] = fmaf(-cf[k * SR].z, z[k + 1], z[k]);
+                        if (k < mm - 1) z[k] = fmaf(-row(k).z, z[k + 1], z[k]);
                 } else {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        if (k < mm) z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * cf[k * SR].z : oR[k];
+                        if (k < mm) z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * row(k).z : oR[k];
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
