@@ -371,38 +371,43 @@ struct BodyCgUr {  // tea_leaf_cg.cuknl:72-137
     double alpha;
     __device__ void setup() { alpha = coef(alpha_p, alpha_v); }
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
-        double rv[4];
+        // every load of the strip before the first store (the arrays may
+        // alias as far as the compiler knows, so it would not hoist them)
+        double uv[4], pv[4], wv[4], rv[4], mv[4], zv[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t i = base + (int64_t)k * pitch;
-                u[i] = fma(alpha, p[i], u[i]);
-                rv[k] = fma(-alpha, w[i], r[i]);
-                r[i] = rv[k];
+                uv[k] = u[i];
+                pv[k] = p[i];
+                wv[k] = w[i];
+                rv[k] = r[i];
+                if (PC == TL_PREC_JAC_DIAG) mv[k] = mi[i];
             }
-        if (PC == TL_PREC_JAC_BLOCK) {
-            double zv[4];
-            strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (k < m) {
-                    z[base + (int64_t)k * pitch] = zv[k];
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                uv[k] = fma(alpha, pv[k], uv[k]);
+                rv[k] = fma(-alpha, wv[k], rv[k]);
+            }
+        if (PC == TL_PREC_JAC_BLOCK) strip_block_solve(dg, ky, cp, bfp, pitch, base, m, rv, zv);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = base + (int64_t)k * pitch;
+                u[i] = uv[k];
+                r[i] = rv[k];
+                if (PC == TL_PREC_JAC_BLOCK) {
+                    z[i] = zv[k];
                     acc[0] = fma(rv[k], zv[k], acc[0]);
-                }
-        } else if (PC == TL_PREC_JAC_DIAG) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (k < m) {
-                    const int64_t i = base + (int64_t)k * pitch;
-                    const double zz = rv[k] * mi[i];
+                } else if (PC == TL_PREC_JAC_DIAG) {
+                    const double zz = rv[k] * mv[k];
                     z[i] = zz;
                     acc[0] = fma(rv[k], zz, acc[0]);
+                } else {
+                    acc[0] = fma(rv[k], rv[k], acc[0]);
                 }
-        } else {
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (k < m) acc[0] = fma(rv[k], rv[k], acc[0]);
-        }
+            }
     }
 };
 
@@ -415,12 +420,17 @@ struct BodyAxpyP {  // p = src + beta p  (tea_leaf_cg.cuknl:141-161, tea_leaf_pp
     double beta;
     __device__ void setup() { beta = coef(beta_p, beta_v); }
     __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
+        double pv[4], sv[4];  // loads first: see BodyCgUr
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t i = base + (int64_t)k * pitch;
-                p[i] = fma(beta, p[i], src[i]);
+                pv[k] = p[i];
+                sv[k] = src[i];
             }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) p[base + (int64_t)k * pitch] = fma(beta, pv[k], sv[k]);
     }
 };
 

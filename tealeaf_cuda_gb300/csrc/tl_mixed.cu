@@ -1036,30 +1036,47 @@ struct BodyPpUr {
         theta_r = (float)(1.0 / sc->theta);
     }
     __device__ void operator()(int64_t b32, int64_t b64, int m, CSum &) const {
-        float rf[4], zf[4];
+        // every load of the strip before the first store (the arrays may
+        // alias as far as the compiler knows, so it would not hoist them)
+        double uv[4], pv[4], wv[4], rv[4];
+        float kyv[4], cpv[4], bfv[4], miv[4], rf[4], zf[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t i = b64 + (int64_t)k * pitch64;
-                u[i] = fma(alpha, p[i], u[i]);
-                const double rv = fma(-alpha, w[i], r[i]);
-                r[i] = rv;
-                rf[k] = (float)rv;
+                const int64_t j = b32 + (int64_t)k * pitch32;
+                uv[k] = u[i];
+                pv[k] = p[i];
+                wv[k] = w[i];
+                rv[k] = r[i];
+                if (PC == TL_PREC_JAC_BLOCK) {
+                    kyv[k] = ky[j];
+                    cpv[k] = cp[j];
+                    bfv[k] = bfp[j];
+                } else if (PC == TL_PREC_JAC_DIAG) {
+                    miv[k] = mi[j];
+                }
+            }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = b64 + (int64_t)k * pitch64;
+                u[i] = fma(alpha, pv[k], uv[k]);
+                rv[k] = fma(-alpha, wv[k], rv[k]);
+                r[i] = rv[k];
+                rf[k] = (float)rv[k];
             }
         if (PC == TL_PREC_JAC_BLOCK) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (k < m) {
-                    const int64_t j = b32 + (int64_t)k * pitch32;
-                    zf[k] = k == 0 ? rf[0] * bfp[j] : fmaf(ky[j], zf[k - 1], rf[k]) * bfp[j];
-                }
+                if (k < m) zf[k] = k == 0 ? rf[0] * bfv[0] : fmaf(kyv[k], zf[k - 1], rf[k]) * bfv[k];
 #pragma unroll
             for (int k = 2; k >= 0; --k)
-                if (k < m - 1) zf[k] = fmaf(-cp[b32 + (int64_t)k * pitch32], zf[k + 1], zf[k]);
+                if (k < m - 1) zf[k] = fmaf(-cpv[k], zf[k + 1], zf[k]);
         } else {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-                if (k < m) zf[k] = PC == TL_PREC_JAC_DIAG ? rf[k] * mi[b32 + (int64_t)k * pitch32] : rf[k];
+                if (k < m) zf[k] = PC == TL_PREC_JAC_DIAG ? rf[k] * miv[k] : rf[k];
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k)
