@@ -80,3 +80,35 @@ def test_training_and_warm_start_gain():
     assert tot["learned_iterations"] < tot["none_iterations"]
     for m in ("prev", "learned"):
         assert tot[m + "_max_summary_rel_diff"] < 1e-10
+
+
+@pytest.mark.parametrize("mode", ["prev", "learned"])
+def test_warm_start_with_mixed_ppcg_keeps_the_fp64_answer(mode):
+    """The headline configuration (FP32-inner PPCG + block-Jacobi under the
+    FP64 outer solve, with a warm start) on a random deck and an untrained
+    network: whatever the start is worth, the answer is plain FP64 CG's."""
+    import ctypes as C
+    n, steps = 256, 4
+    deck = learned.random_deck(123, n, steps)
+    plain = learned.solve_with("none", None, deck, steps)
+    params = np.ascontiguousarray(learned.init_params(7, head_scale=1.0), dtype=np.float32)
+    cfg = tl.parse_deck(deck)
+    cfg.solver = tl.SOLVER_PPCG
+    cfg.precond = tl.PREC_JAC_BLOCK
+    cfg.ppcg_inner_steps = 10
+    cfg.precision = tl.PRECISION_MIXED
+    cfg.warm_start = learned.WARM[mode]
+    out = []
+    with tl.Chunk(cfg) as ch:
+        ch.start()
+        if mode == "learned":
+            assert tl.load().tl_set_warm_start_model(ch._h, C.c_void_p(params.ctypes.data), params.size) == 0
+        for _ in range(steps):
+            info = ch.timestep()
+            out.append((info, ch.field_summary()))
+    for step, ((info, fs), ref) in enumerate(zip(out, plain), start=1):
+        assert info["status"] == 0, step
+        if step > 1:
+            assert info["warm_used"] == 1, step  # d_prev exists from the second step on
+        for a, b in zip(fs, ref["summary"]):
+            assert a == pytest.approx(b, rel=1e-10), step
