@@ -1251,7 +1251,10 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
     cudaStream_t s = c->stream;
     const int pc = c->cfg.precond;
     int rc;
-    const int fuse = c->inner_fuse < 1 ? 1 : (c->inner_fuse > kFusedMax ? kFusedMax : c->inner_fuse);
+    // the fused kernel addresses FP32 fields with 32-bit offsets; fields of
+    // 2^31 elements or more take the one-kernel-per-step path (64-bit)
+    const bool fits32 = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows < ((size_t)1 << 31);
+    const int fuse = !fits32 ? 1 : c->inner_fuse < 1 ? 1 : (c->inner_fuse > kFusedMax ? kFusedMax : c->inner_fuse);
     if (fuse > 1) {
         float *rt[2] = {mx->rtemp, mx->rtemp2};
         const int passes = (inner + fuse - 1) / fuse;
