@@ -80,6 +80,8 @@ BYTES_PER_CELL = {
     "field_summary": 32,
     "finalise": 24,
     "ppcg_p": 24,        # read z, p; write p
+    "ppcg_update_r": 48,  # read sd, Kx, Ky, diag, rtemp; write rtemp
+    "cheby_calc_u": 24,  # read u, p; write u
     "copy": 16,          # read src; write dst
     "ppcg_w_zr": 64,     # read p, Kx, Ky, diag, r, z; write w, r_store
     "ppcg_rrn": 24,      # read r, r_store, z
@@ -110,6 +112,14 @@ def bytes_per_cell(kernel, precond):
         # 1/b of the strip solve); write sd', rtemp, utemp (an inner step
         # before the last)
         return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
+    if kernel == "cheby_p":
+        # read u, Kx, Ky, diag, u0, p + the preconditioner (Mi; or cp, bfp);
+        # write w, r, p
+        return {"none": 72, "jac_diag": 80, "jac_block": 88}[precond]
+    if kernel == "ppcg_sd":
+        # read rtemp, sd, utemp + the preconditioner (Mi; or diag, Ky, cp,
+        # bfp); write sd, utemp
+        return {"none": 40, "jac_diag": 48, "jac_block": 72}[precond]
     if kernel == "mixed_ur":
         # read d, p, r, w + the preconditioner (Mi; or Ky, cp, bfp); write d, r, z
         return {"none": 28, "jac_diag": 32, "jac_block": 40}[precond]
