@@ -124,6 +124,18 @@ def test_flags_match_oracle(extra):
     recs, steps = compare_to_oracle(deck)
 
 
+@pytest.mark.parametrize("solver", ["ppcg", "cheby"])
+@pytest.mark.parametrize("extra", [{"reflective_boundary": True},
+                                   {"tl_coefficient_inverse_density": True},
+                                   {"halo_depth": 2}])
+def test_flags_with_chebyshev_and_ppcg_match_oracle(solver, extra):
+    """The same flags under the polynomial solvers (halo_depth 2 takes
+    PPCG's matrix-powers inner loop, tea_leaf_ppcg.f90:199-221)."""
+    deck = decks.make_deck(x_cells=50, y_cells=44, end_step=2, tl_preconditioner_type="jac_diag",
+                           **SOLVERS[solver], **extra)
+    compare_to_oracle(deck, its_tol=10 if solver == "cheby" else 1)
+
+
 def test_determinism():
     deck = decks.make_deck(x_cells=96, y_cells=80, end_step=2, tl_preconditioner_type="jac_diag")
     a, _ = gpu_run(deck)
