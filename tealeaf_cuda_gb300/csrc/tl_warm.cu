@@ -4,18 +4,24 @@
 // (tea_leaf_common.cuknl:28-34); the plain start is u = u^n, whose residual
 // is r0 = u^n - A u^n, and the exact correction is du = A^-1 r0.  A warm
 // start adds a combination of search directions to u^n:
-//   d_net  = the residual network's prediction of du (tl_warm_start learned)
-//   d_prev = u^n - u^(n-1), the previous step's increment (both modes)
+//   d_net   = the residual network's prediction of du (tl_warm_start learned)
+//   d_1..d_k = the last k increments u^(n-j+1) - u^(n-j) (both modes, k <= 4)
 // with the coefficients that minimise the energy
-//   phi(u) = 1/2 u.Au - u.u^n   over   u = u^n + a d_net + b d_prev,
-// i.e. the 2x2 Galerkin system [d.Ad'] (a, b) = [d.r0].  Because A is SPD,
-// phi - phi(u*) = 1/2 |u - u*|_A^2, so the chosen start never has a larger
-// A-norm error than the plain one.  The solve's exit test stays tl_eps times
-// the plain start's residual, so the answer meets the same tolerance.
+//   phi(u) = 1/2 u.Au - u.u^n   over   u = u^n + sum_i c_i d_i,
+// i.e. the Galerkin system [d_i.Ad_j] c = [d_i.r0] (projection onto previous
+// solutions, as for sequences of right-hand sides: with A fixed, the
+// increments are repeated applications of A^-1, so they span the smooth,
+// slowly decaying part of the next correction).  The small system is solved
+// on the host by A-orthonormalising the directions (Gram-Schmidt in the
+// inner product G, twice, dropping directions that are numerically
+// dependent).  Because A is SPD, phi - phi(u*) = 1/2 |u - u*|_A^2, so the
+// chosen start never has a larger A-norm error than the plain one.  The
+// solve's exit test stays tl_eps times the plain start's residual, so the
+// answer meets the same tolerance.
 //
 // Network input per cell (channels 0..6, BF16, NHWC, 1-pixel zero halo):
 //   u^n / max|u^n|, log density, log1p(Kx west face), log1p(Ky south face),
-//   100 dt, r0 / max|r0|, d_prev / max|r0|;
+//   100 dt, r0 / max|r0|, d_1 / max|r0| (the latest increment);
 // output channel 0 is du / max|r0| (the network is linear-equivariant in the
 // residual's scale).
 //
@@ -49,18 +55,24 @@ constexpr int kCout[kLayers] = {32, 32, 32, 32, 32, 16};
 constexpr int kInputs = 7;          // network input channels in use
 constexpr int kFeatures = kInputs + 1;  // + the training target
 constexpr int kGramBlocks = 608;    // 152 SMs x 4
-constexpr int kGramSums = 6;        // Gnn, Gnp, Gpp, bn, bp, r0.r0
+constexpr int kHist = 4;            // previous increments kept
+constexpr int kMaxDirs = kHist + 1; // + the network's direction
+constexpr int kGramPairs = kMaxDirs * (kMaxDirs + 1) / 2;
+constexpr int kGramSums = kGramPairs + kMaxDirs + 1;  // d_i.Ad_j (i <= j), d_i.r0, r0.r0
 constexpr float kClamp = 64.f;      // bound of the scaled inputs
 
 struct Warm {
     // previous-step tracking (both warm start modes)
     double *uprev;              // u^(n-1), field layout
-    double *dprev;              // u^n - u^(n-1) of the current step
+    double *hist[kHist];        // ring of the last increments (zero halo)
+    int nhist;                  // increments in the ring
+    int head;                   // slot the next increment goes to
+    int cur;                    // slot holding the current step's increment
     double *dnet;               // network direction (field layout, zero halo)
     double *r0;                 // scratch: u^n - A u^n
     double *partials;           // [kGramBlocks][kGramSums]
     float *scale;               // device [0] max|u^n|, [1] max|r0|
-    bool have_prev;
+    bool have_prev;             // u^(n-1) is known
     std::vector<void *> allocs;
     // the network (learned mode)
     bool model;
@@ -188,31 +200,45 @@ __global__ void k_dnet(Geo g, const float *__restrict__ y, int nxp, const float 
     }
 }
 
+// the search directions of one warm start (null beyond n)
+struct Dirs {
+    const double *d[kMaxDirs];
+    int n;
+};
+
+// index of d_i.Ad_j (i <= j) among the Gram sums
+__host__ __device__ constexpr int pair_index(int i, int j) { return i * kMaxDirs - i * (i - 1) / 2 + (j - i); }
+
 // Gram entries of the Galerkin system, per CTA in a fixed order:
-// [dn.Adn, dn.Adp, dp.Adp, dn.r0, dp.r0, r0.r0]; a null direction counts 0
-__global__ void __launch_bounds__(256) k_gram(Geo g, const double *__restrict__ dn,
-                                              const double *__restrict__ dp, const double *__restrict__ r0,
+// d_i.Ad_j for i <= j, then d_i.r0, then r0.r0
+__global__ void __launch_bounds__(256) k_gram(Geo g, Dirs D, const double *__restrict__ r0,
                                               const double *__restrict__ dg, const double *__restrict__ kx,
                                               const double *__restrict__ ky, double *__restrict__ partials) {
-    double s[kGramSums] = {0, 0, 0, 0, 0, 0};
+    double s[kGramSums];
+#pragma unroll
+    for (int q = 0; q < kGramSums; ++q) s[q] = 0.0;
     const long long n = (long long)g.nx * g.ny;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         int i, j;
         const int64_t c = cell_of(g, k, &i, &j);
         const double r = r0[c];
-        s[5] = fma(r, r, s[5]);
-        if (dn) {
-            const double an = apply_a(dn, dg, kx, ky, c, g.pitch);
-            s[0] = fma(dn[c], an, s[0]);
-            s[3] = fma(dn[c], r, s[3]);
-            if (dp) s[1] = fma(dp[c], an, s[1]);
+        double dv[kMaxDirs], av[kMaxDirs];
+#pragma unroll
+        for (int a = 0; a < kMaxDirs; ++a) {
+            dv[a] = av[a] = 0.0;
+            if (a < D.n) {
+                dv[a] = D.d[a][c];
+                av[a] = apply_a(D.d[a], dg, kx, ky, c, g.pitch);
+            }
         }
-        if (dp) {
-            const double ap = apply_a(dp, dg, kx, ky, c, g.pitch);
-            s[2] = fma(dp[c], ap, s[2]);
-            s[4] = fma(dp[c], r, s[4]);
+#pragma unroll
+        for (int a = 0; a < kMaxDirs; ++a) {
+#pragma unroll
+            for (int b = a; b < kMaxDirs; ++b) s[pair_index(a, b)] = fma(dv[a], av[b], s[pair_index(a, b)]);
+            s[kGramPairs + a] = fma(dv[a], r, s[kGramPairs + a]);
         }
+        s[kGramSums - 1] = fma(r, r, s[kGramSums - 1]);
     }
     __shared__ double red[8][kGramSums];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -230,17 +256,21 @@ __global__ void __launch_bounds__(256) k_gram(Geo g, const double *__restrict__ 
     }
 }
 
-// u = u0 + a dn + b dp on the interior
-__global__ void k_combine(Geo g, const double *__restrict__ u0, const double *__restrict__ dn, double a,
-                          const double *__restrict__ dp, double b, double *__restrict__ u) {
+struct Coefs {
+    double c[kMaxDirs];
+};
+
+// u = u0 + sum_i c_i d_i on the interior
+__global__ void k_combine(Geo g, const double *__restrict__ u0, Dirs D, Coefs C, double *__restrict__ u) {
     const long long n = (long long)g.nx * g.ny;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         int i, j;
         const int64_t c = cell_of(g, k, &i, &j);
         double v = u0[c];
-        if (dn) v = fma(a, dn[c], v);
-        if (dp) v = fma(b, dp[c], v);
+#pragma unroll
+        for (int a = 0; a < kMaxDirs; ++a)
+            if (a < D.n) v = fma(C.c[a], D.d[a][c], v);
         u[c] = v;
     }
 }
@@ -280,7 +310,8 @@ int warm_state(Chunk *c, Warm **out) {
     cudaStream_t s = c->stream;
     int rc;
     void *p;
-    double **fields[4] = {&w->uprev, &w->dprev, &w->dnet, &w->r0};
+    double **fields[3 + kHist] = {&w->uprev, &w->dnet, &w->r0, &w->hist[0], &w->hist[1], &w->hist[2], &w->hist[3]};
+    static_assert(kHist == 4, "the field list names every history slot");
     for (double **f : fields) {
         if ((rc = dmalloc(w->allocs, &p, bytes, s))) return rc;
         *f = (double *)p + off;
@@ -300,12 +331,13 @@ int scales(Chunk *c, Warm *w) {
     return launched(c, "absmax launch");
 }
 
-// dnet = network(features) (call after common_init, with r0 and dprev current)
+// dnet = network(features) (call after common_init, with r0 and the current
+// increment in place)
 int net_direction(Chunk *c, Warm *w) {
     cudaStream_t s = c->stream;
     int rc;
-    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->dprev, c->density, c->kx, c->ky, w->scale,
-                                    c->dt, w->x, w->nxp, nullptr);
+    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->hist[w->cur], c->density, c->kx, c->ky,
+                                    w->scale, c->dt, w->x, w->nxp, nullptr);
     if ((rc = launched(c, "features launch"))) return rc;
     bf16 *h = w->h0, *hn = w->h1;
     if ((rc = tl_nn_conv(0, 16, 32, w->x, w->wf[0], w->bias[0], nullptr, h, w->pre, nullptr, 1, c->ny,
@@ -326,38 +358,52 @@ int net_direction(Chunk *c, Warm *w) {
     return launched(c, "network direction");
 }
 
-// coefficients (a, b) minimising phi over u0 + a dn + b dp; returns the
-// energy decrease times two (a bn + b bp), 0 when no direction helps
-double galerkin(const double *S, bool use_n, bool use_p, double *a, double *b) {
-    const double gnn = S[0], gnp = S[1], gpp = S[2], bn = S[3], bp = S[4];
-    *a = 0.0;
-    *b = 0.0;
-    const bool ok_n = use_n && gnn > 0.0 && isfinite(gnn) && isfinite(bn);
-    const bool ok_p = use_p && gpp > 0.0 && isfinite(gpp) && isfinite(bp);
-    double best = 0.0;
-    if (ok_n && ok_p) {
-        const double det = gnn * gpp - gnp * gnp;
-        if (isfinite(det) && det > 1e-12 * gnn * gpp) {
-            const double x = (bn * gpp - bp * gnp) / det, y = (gnn * bp - gnp * bn) / det;
-            const double gain = x * bn + y * bp;
-            if (isfinite(gain) && gain > 0.0) {
-                *a = x;
-                *b = y;
-                return gain;
+// coefficients c minimising phi over u0 + sum_i c_i d_i (n directions)
+// from the Gram sums S: Gram-Schmidt in the inner product G_ij = d_i.Ad_j,
+// done twice, dropping a direction whose remaining G-norm^2 is below 1e-10
+// of its own (numerically dependent on the earlier ones); returns twice the
+// energy decrease, 0 when no direction helps
+double project(const double *S, int n, double *coef) {
+    double G[kMaxDirs][kMaxDirs], bv[kMaxDirs], Q[kMaxDirs][kMaxDirs];
+    for (int i = 0; i < n; ++i) {
+        coef[i] = 0.0;
+        bv[i] = S[kGramPairs + i];
+        for (int j = i; j < n; ++j) G[i][j] = G[j][i] = S[pair_index(i, j)];
+    }
+    auto ip = [&](const double *x, const double *y) {
+        double t = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) t += x[i] * G[i][j] * y[j];
+        return t;
+    };
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        if (!(G[i][i] > 0.0) || !isfinite(G[i][i]) || !isfinite(bv[i])) continue;
+        double v[kMaxDirs] = {0, 0, 0, 0, 0};
+        v[i] = 1.0;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int q = 0; q < m; ++q) {
+                const double h = ip(Q[q], v);
+                for (int k = 0; k < n; ++k) v[k] -= h * Q[q][k];
             }
-        }
+        const double nrm2 = ip(v, v);
+        if (!(nrm2 > 1e-10 * G[i][i]) || !isfinite(nrm2)) continue;
+        const double inv = 1.0 / sqrt(nrm2);
+        for (int k = 0; k < n; ++k) Q[m][k] = v[k] * inv;
+        ++m;
     }
-    if (ok_n && bn * bn / gnn > best) {
-        best = bn * bn / gnn;
-        *a = bn / gnn;
-        *b = 0.0;
+    double gain = 0.0;
+    for (int q = 0; q < m; ++q) {
+        double t = 0.0;
+        for (int k = 0; k < n; ++k) t += Q[q][k] * bv[k];
+        gain += t * t;
+        for (int k = 0; k < n; ++k) coef[k] += t * Q[q][k];
     }
-    if (ok_p && bp * bp / gpp > best) {
-        best = bp * bp / gpp;
-        *a = 0.0;
-        *b = bp / gpp;
+    if (!isfinite(gain)) {
+        for (int k = 0; k < n; ++k) coef[k] = 0.0;
+        return 0.0;
     }
-    return best;
+    return gain;
 }
 
 }  // namespace
@@ -372,7 +418,10 @@ void warm_free(Chunk *c) {
 }
 
 void warm_reset(Chunk *c) {
-    if (Warm *w = warm_of(c)) w->have_prev = false;
+    if (Warm *w = warm_of(c)) {
+        w->have_prev = false;
+        w->nhist = w->head = w->cur = 0;
+    }
 }
 
 long long warm_param_count() {
@@ -438,18 +487,29 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
     if ((rc = launch_residual(c, kEpiStore))) return rc;
     if ((rc = launch_copy(c, w->r0, c->r, false))) return rc;
     const bool have_prev = w->have_prev;
-    k_prev<<<1216, 256, 0, s>>>(c->g, c->u0, w->uprev, w->dprev, have_prev ? 1 : 0);
+    // the increment of this step, u^n - u^(n-1), into the history ring
+    w->cur = w->head;
+    k_prev<<<1216, 256, 0, s>>>(c->g, c->u0, w->uprev, w->hist[w->cur], have_prev ? 1 : 0);
     if ((rc = launched(c, "previous step launch"))) return rc;
+    if (have_prev) {
+        w->nhist = w->nhist < kHist ? w->nhist + 1 : kHist;
+        w->head = (w->head + 1) % kHist;
+    }
     w->have_prev = true;
     if (learned) {
         if ((rc = scales(c, w))) return rc;
         if ((rc = net_direction(c, w))) return rc;
     }
-    const double *dn = learned ? w->dnet : nullptr;
-    const double *dp = have_prev ? w->dprev : nullptr;
-    double S[kGramSums] = {0, 0, 0, 0, 0, 0};
-    if (dn || dp) {
-        k_gram<<<kGramBlocks, 256, 0, s>>>(c->g, dn, dp, w->r0, c->diag, c->kx, c->ky, w->partials);
+    // directions: the network's, then the increments from the newest
+    Dirs D;
+    D.n = 0;
+    for (int a = 0; a < kMaxDirs; ++a) D.d[a] = nullptr;
+    if (learned) D.d[D.n++] = w->dnet;
+    for (int j = 0; j < w->nhist; ++j) D.d[D.n++] = w->hist[(w->cur - j + kHist) % kHist];
+    double S[kGramSums];
+    for (int q = 0; q < kGramSums; ++q) S[q] = 0.0;
+    if (D.n > 0) {
+        k_gram<<<kGramBlocks, 256, 0, s>>>(c->g, D, w->r0, c->diag, c->kx, c->ky, w->partials);
         if ((rc = launched(c, "gram launch"))) return rc;
         std::vector<double> part((size_t)kGramBlocks * kGramSums);
         TL_CUDA(cudaMemcpyAsync(part.data(), w->partials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
@@ -462,10 +522,11 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
     const double rr0 = c->sc_host->sum[0];
     *r0 = sqrt(fabs(rr0));
     *rr = rr0;
-    double a = 0.0, b = 0.0;
-    const double gain = galerkin(S, dn != nullptr, dp != nullptr, &a, &b);
+    Coefs C;
+    for (int a = 0; a < kMaxDirs; ++a) C.c[a] = 0.0;
+    const double gain = D.n > 0 ? project(S, D.n, C.c) : 0.0;
     if (!(gain > 0.0)) return TL_OK;  // the plain start: u = u^n, r = r0
-    k_combine<<<1216, 256, 0, s>>>(c->g, c->u0, a != 0.0 ? dn : nullptr, a, b != 0.0 ? dp : nullptr, b, c->u);
+    k_combine<<<1216, 256, 0, s>>>(c->g, c->u0, D, C, c->u);
     if ((rc = launched(c, "warm start combine"))) return rc;
     if ((rc = launch_residual(c, kEpiStore))) return rc;
     if ((rc = chunk_sync_scalars(c))) return rc;
@@ -489,8 +550,8 @@ int warm_features(Chunk *c, float *dst) {
     k_resid0<<<1216, 256, 0, s>>>(c->g, c->u0, c->diag, c->kx, c->ky, w->r0);
     if ((rc = launched(c, "residual launch"))) return rc;
     if ((rc = scales(c, w))) return rc;
-    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->dprev, c->density, c->kx, c->ky, w->scale,
-                                    c->dt, nullptr, 0, dst);
+    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->hist[w->cur], c->density, c->kx, c->ky,
+                                    w->scale, c->dt, nullptr, 0, dst);
     if ((rc = launched(c, "features launch"))) return rc;
     TL_CUDA(cudaStreamSynchronize(s));
     return TL_OK;
