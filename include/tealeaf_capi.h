@@ -219,17 +219,17 @@ int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long p
 
 /* ------------------------------------------------ warm starts
  * No reference counterpart.  With cfg.warm_start set, tl_timestep starts from
- *   u = u^n + a d_net + b d_prev
- * where d_prev = u^n - u^{n-1} (the previous step's increment; absent on the
- * first step after tl_start) and d_net is a residual network's prediction of
- * the correction A^-1 (u^n - A u^n) (TL_WARM_LEARNED only).  (a, b) solve the
- * 2x2 Galerkin system that minimises the energy 1/2 u.Au - u.u^n, so the
+ *   u = u^n + sum_i c_i d_i
+ * over the last (up to four) increments d_j = u^{n-j+1} - u^{n-j} (none on
+ * the first step after tl_start) and, for TL_WARM_LEARNED, a residual
+ * network's prediction of the correction A^-1 (u^n - A u^n).  The c_i solve
+ * the Galerkin system that minimises the energy 1/2 u.Au - u.u^n, so the
  * start's A-norm error is never above the plain start's; the exit test stays
  * tl_eps * (residual of the plain start u = u^n).
  *
  * The network: six 3x3 convolutions (32 channels, GELU, BF16 tensor-core
  * kernels).  Inputs per cell: u^n/max|u^n|, log density, log1p Kx, log1p Ky,
- * 100 dt, r0/max|r0|, d_prev/max|r0| (r0 = u^n - A u^n); output: the
+ * 100 dt, r0/max|r0|, d_1/max|r0| (r0 = u^n - A u^n); output: the
  * correction / max|r0|.  Parameters: FP32, flat, per layer W[9][coutp][cin]
  * then b[coutp]; layers (cin, coutp) = (16,32) GELU, 4 x (32,32)
  * x + GELU(conv x), (32,16) linear head (output channel 0).  A model file is

@@ -4,11 +4,12 @@ kernels (tl_nn_* in csrc/tl_conv.cu), model files, and the evaluation of
 what the warm starts save over the plain start.
 
 Network (tl_warm.cu): inputs (u^n / max|u^n|, log density, log1p Kx,
-log1p Ky, 100 dt, r0 / max|r0|, d_prev / max|r0|) with r0 = u^n - A u^n and
-d_prev = u^n - u^{n-1}; six 3x3 convolutions of 32 channels (GELU, four
+log1p Ky, 100 dt, r0 / max|r0|, d_1 / max|r0|) with r0 = u^n - A u^n and
+d_1 = u^n - u^{n-1}; six 3x3 convolutions of 32 channels (GELU, four
 residual blocks); output (u^{n+1} - u^n) / max|r0|.  The solve starts from
-u^n + a d_net + b d_prev with the energy-minimising (a, b) and keeps
-tl_eps * (plain start residual) as its exit test.  Torch only allocates
+u^n plus the energy-minimising combination of the network's output and the
+last four increments, and keeps tl_eps * (plain start residual) as its exit
+test.  Torch only allocates
 device buffers here; every FLOP of the network runs in the library's
 kernels.
 """

@@ -65,7 +65,7 @@ def test_gradients_match_oracle():
 
 def test_training_and_warm_start_gain():
     """Train on 24 decks at 512^2, then count CG iterations on three held-out
-    decks from the plain start, the previous-step start and the learned one;
+    decks from the plain start, the increment-history start and the learned one;
     every start must give the same answer to the solve's tolerance."""
     n, steps = 512, 6
     data, iters = learned.trajectory_crops(range(100, 124), n, steps, crops_per_step=4)
@@ -109,6 +109,6 @@ def test_warm_start_with_mixed_ppcg_keeps_the_fp64_answer(mode):
     for step, ((info, fs), ref) in enumerate(zip(out, plain), start=1):
         assert info["status"] == 0, step
         if step > 1:
-            assert info["warm_used"] == 1, step  # d_prev exists from the second step on
+            assert info["warm_used"] == 1, step  # an increment exists from the second step on
         for a, b in zip(fs, ref["summary"]):
             assert a == pytest.approx(b, rel=1e-10), step
