@@ -228,9 +228,11 @@ int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long p
  * tl_eps * (residual of the plain start u = u^n).
  *
  * The network: six 3x3 convolutions (32 channels, GELU, BF16 tensor-core
- * kernels).  Inputs per cell: u^n/max|u^n|, log density, log1p Kx, log1p Ky,
- * 100 dt, r0/max|r0|, d_1/max|r0| (r0 = u^n - A u^n); output: the
- * correction / max|r0|.  Parameters: FP32, flat, per layer W[9][coutp][cin]
+ * kernels).  It corrects the increments' own projection u_h: inputs per cell
+ * u^n/max|u^n|, log density, log1p Kx, log1p Ky, 100 dt, r_h/max|r_h|,
+ * d_1/max|r_h| (r_h = u^n - A u_h); output: (u^{n+1} - u_h)/max|r_h|; the
+ * start is then projected jointly over its output and the increments.
+ * Parameters: FP32, flat, per layer W[9][coutp][cin]
  * then b[coutp]; layers (cin, coutp) = (16,32) GELU, 4 x (32,32)
  * x + GELU(conv x), (32,16) linear head (output channel 0).  A model file is
  * the 8 bytes "TLWS0001", an int64 parameter count, then the FP32
@@ -238,8 +240,8 @@ int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long p
 long long tl_warm_start_param_count(void);
 int tl_set_warm_start_model(tl_chunk_t *ch, const float *params, long long n);
 /* training data of the step just solved (which must have run with a warm
- * start, so that u^{n-1} is tracked): FP32 [ny][nx][8] at device dst = the
- * seven network inputs and the target (u^{n+1} - u^n)/max|r0| */
+ * start, so that the increments are tracked): FP32 [ny][nx][8] at device
+ * dst = the seven network inputs and the target (u^{n+1} - u_h)/max|r_h| */
 int tl_warm_start_features(tl_chunk_t *ch, float *dst);
 
 /* Network kernels on caller-owned device buffers (NHWC BF16 activations with

@@ -19,11 +19,15 @@
 // solve's exit test stays tl_eps times the plain start's residual, so the
 // answer meets the same tolerance.
 //
-// Network input per cell (channels 0..6, BF16, NHWC, 1-pixel zero halo):
+// The network corrects what the history leaves: its input residual is that
+// of the history start u_h = u^n + (the increments' projection alone),
+// r_h = u^n - A u_h, and it predicts A^-1 r_h; the final start is the joint
+// projection over the network's direction and the increments.  Input per
+// cell (channels 0..6, BF16, NHWC, 1-pixel zero halo):
 //   u^n / max|u^n|, log density, log1p(Kx west face), log1p(Ky south face),
-//   100 dt, r0 / max|r0|, d_1 / max|r0| (the latest increment);
-// output channel 0 is du / max|r0| (the network is linear-equivariant in the
-// residual's scale).
+//   100 dt, r_h / max|r_h|, d_1 / max|r_h| (the latest increment);
+// output channel 0 is (u^{n+1} - u_h) / max|r_h| (the network is
+// linear-equivariant in the residual's scale).
 //
 // Model parameters (FP32, flat, in this order per layer: W [9][coutp][cin]
 // then b [coutp]):
@@ -69,7 +73,9 @@ struct Warm {
     int head;                   // slot the next increment goes to
     int cur;                    // slot holding the current step's increment
     double *dnet;               // network direction (field layout, zero halo)
-    double *r0;                 // scratch: u^n - A u^n
+    double *r0;                 // u^n - A u^n (the plain start's residual)
+    double *ustart;             // u_h, the history start of the current step
+    double *rh;                 // u^n - A u_h
     double *partials;           // [kGramBlocks][kGramSums]
     float *scale;               // device [0] max|u^n|, [1] max|r0|
     bool have_prev;             // u^(n-1) is known
@@ -125,15 +131,16 @@ __global__ void k_absmax2(Geo g, const double *__restrict__ a, const double *__r
     }
 }
 
-// r0 = u0 - A u0 on the interior
-__global__ void k_resid0(Geo g, const double *__restrict__ u0, const double *__restrict__ dg,
-                         const double *__restrict__ kx, const double *__restrict__ ky, double *__restrict__ r0) {
+// r = u0 - A v on the interior
+__global__ void k_resid_of(Geo g, const double *__restrict__ u0, const double *__restrict__ v,
+                           const double *__restrict__ dg, const double *__restrict__ kx,
+                           const double *__restrict__ ky, double *__restrict__ r) {
     const long long n = (long long)g.nx * g.ny;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         int i, j;
         const int64_t c = cell_of(g, k, &i, &j);
-        r0[c] = u0[c] - apply_a(u0, dg, kx, ky, c, g.pitch);
+        r[c] = u0[c] - apply_a(v, dg, kx, ky, c, g.pitch);
     }
 }
 
@@ -155,9 +162,10 @@ __device__ __forceinline__ float clampf(float v) { return fminf(fmaxf(v, -kClamp
 
 // network inputs of cell (i, j), as BF16 into the padded NHWC input
 // (x != nullptr) and/or as FP32 [ny][nx][kFeatures] with the target
-// (u - u0) / max|r0| (f != nullptr)
+// (u - ubase) / max|rr| (f != nullptr); rr is the residual of ubase
 __global__ void k_features(Geo g, const double *__restrict__ u0, const double *__restrict__ u,
-                           const double *__restrict__ r0, const double *__restrict__ dprev,
+                           const double *__restrict__ ubase, const double *__restrict__ rr,
+                           const double *__restrict__ dprev,
                            const double *__restrict__ density, const double *__restrict__ kx,
                            const double *__restrict__ ky, const float *__restrict__ scale, double dt,
                            bf16 *__restrict__ x, int nxp, float *__restrict__ f) {
@@ -173,7 +181,7 @@ __global__ void k_features(Geo g, const double *__restrict__ u0, const double *_
         v[2] = log1pf((float)kx[c]);
         v[3] = log1pf((float)ky[c]);
         v[4] = (float)(100.0 * dt);
-        v[5] = clampf((float)(r0[c] / sr));
+        v[5] = clampf((float)(rr[c] / sr));
         v[6] = clampf((float)(dprev[c] / sr));
         if (x) {
             bf16 *d = x + (((int64_t)(j + 1)) * (nxp + 2) + i + 1) * 16;
@@ -182,7 +190,7 @@ __global__ void k_features(Geo g, const double *__restrict__ u0, const double *_
         if (f) {
             float *d = f + k * kFeatures;
             for (int q = 0; q < kInputs; ++q) d[q] = v[q];
-            d[kInputs] = (float)((u[c] - u0[c]) / sr);
+            d[kInputs] = (float)((u[c] - ubase[c]) / sr);
         }
     }
 }
@@ -310,7 +318,8 @@ int warm_state(Chunk *c, Warm **out) {
     cudaStream_t s = c->stream;
     int rc;
     void *p;
-    double **fields[3 + kHist] = {&w->uprev, &w->dnet, &w->r0, &w->hist[0], &w->hist[1], &w->hist[2], &w->hist[3]};
+    double **fields[5 + kHist] = {&w->uprev, &w->dnet,    &w->r0,      &w->ustart, &w->rh,
+                                  &w->hist[0], &w->hist[1], &w->hist[2], &w->hist[3]};
     static_assert(kHist == 4, "the field list names every history slot");
     for (double **f : fields) {
         if ((rc = dmalloc(w->allocs, &p, bytes, s))) return rc;
@@ -324,20 +333,19 @@ int warm_state(Chunk *c, Warm **out) {
     return TL_OK;
 }
 
-// max|u0| and max|r0| into w->scale
+// max|u0| and max|r_h| into w->scale
 int scales(Chunk *c, Warm *w) {
     TL_CUDA(cudaMemsetAsync(w->scale, 0, 2 * sizeof(float), c->stream));
-    k_absmax2<<<kGramBlocks, 256, 0, c->stream>>>(c->g, c->u0, w->r0, w->scale);
+    k_absmax2<<<kGramBlocks, 256, 0, c->stream>>>(c->g, c->u0, w->rh, w->scale);
     return launched(c, "absmax launch");
 }
 
-// dnet = network(features) (call after common_init, with r0 and the current
-// increment in place)
+// dnet = network(features) (with u_h, r_h and the current increment in place)
 int net_direction(Chunk *c, Warm *w) {
     cudaStream_t s = c->stream;
     int rc;
-    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->hist[w->cur], c->density, c->kx, c->ky,
-                                    w->scale, c->dt, w->x, w->nxp, nullptr);
+    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->ustart, w->rh, w->hist[w->cur], c->density, c->kx,
+                                    c->ky, w->scale, c->dt, w->x, w->nxp, nullptr);
     if ((rc = launched(c, "features launch"))) return rc;
     bf16 *h = w->h0, *hn = w->h1;
     if ((rc = tl_nn_conv(0, 16, 32, w->x, w->wf[0], w->bias[0], nullptr, h, w->pre, nullptr, 1, c->ny,
@@ -404,6 +412,28 @@ double project(const double *S, int n, double *coef) {
         return 0.0;
     }
     return gain;
+}
+
+// Gram sums of the directions D (k_gram, partials summed on the host in CTA
+// order) and their projection: coefficients into *C, twice the energy
+// decrease into *gain (0 when D is empty or nothing helps)
+int gram_project(Chunk *c, Warm *w, const Dirs &D, Coefs *C, double *gain) {
+    for (int a = 0; a < kMaxDirs; ++a) C->c[a] = 0.0;
+    *gain = 0.0;
+    if (D.n == 0) return TL_OK;
+    cudaStream_t s = c->stream;
+    int rc;
+    k_gram<<<kGramBlocks, 256, 0, s>>>(c->g, D, w->r0, c->diag, c->kx, c->ky, w->partials);
+    if ((rc = launched(c, "gram launch"))) return rc;
+    std::vector<double> part((size_t)kGramBlocks * kGramSums);
+    TL_CUDA(cudaMemcpyAsync(part.data(), w->partials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s));
+    TL_CUDA(cudaStreamSynchronize(s));
+    double S[kGramSums];
+    for (int q = 0; q < kGramSums; ++q) S[q] = 0.0;
+    for (int b = 0; b < kGramBlocks; ++b)
+        for (int q = 0; q < kGramSums; ++q) S[q] += part[(size_t)b * kGramSums + q];
+    *gain = project(S, D.n, C->c);
+    return TL_OK;
 }
 
 }  // namespace
@@ -496,35 +526,36 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
         w->head = (w->head + 1) % kHist;
     }
     w->have_prev = true;
+    // the history start u_h: the increments' projection alone
+    Dirs H;
+    H.n = 0;
+    for (int a = 0; a < kMaxDirs; ++a) H.d[a] = nullptr;
+    for (int j = 0; j < w->nhist; ++j) H.d[H.n++] = w->hist[(w->cur - j + kHist) % kHist];
+    Coefs CH;
+    double gh = 0.0;
+    if ((rc = gram_project(c, w, H, &CH, &gh))) return rc;
+    if (gh > 0.0) k_combine<<<1216, 256, 0, s>>>(c->g, c->u0, H, CH, w->ustart);
+    else k_combine<<<1216, 256, 0, s>>>(c->g, c->u0, Dirs{{nullptr}, 0}, CH, w->ustart);
+    if ((rc = launched(c, "history start"))) return rc;
+    Dirs D = H;
+    Coefs C = CH;
+    double gain = gh;
     if (learned) {
+        // the network corrects u_h: input r_h = u^n - A u_h; then the joint
+        // projection over its direction and the increments
+        k_resid_of<<<1216, 256, 0, s>>>(c->g, c->u0, w->ustart, c->diag, c->kx, c->ky, w->rh);
+        if ((rc = launched(c, "history residual"))) return rc;
         if ((rc = scales(c, w))) return rc;
         if ((rc = net_direction(c, w))) return rc;
-    }
-    // directions: the network's, then the increments from the newest
-    Dirs D;
-    D.n = 0;
-    for (int a = 0; a < kMaxDirs; ++a) D.d[a] = nullptr;
-    if (learned) D.d[D.n++] = w->dnet;
-    for (int j = 0; j < w->nhist; ++j) D.d[D.n++] = w->hist[(w->cur - j + kHist) % kHist];
-    double S[kGramSums];
-    for (int q = 0; q < kGramSums; ++q) S[q] = 0.0;
-    if (D.n > 0) {
-        k_gram<<<kGramBlocks, 256, 0, s>>>(c->g, D, w->r0, c->diag, c->kx, c->ky, w->partials);
-        if ((rc = launched(c, "gram launch"))) return rc;
-        std::vector<double> part((size_t)kGramBlocks * kGramSums);
-        TL_CUDA(cudaMemcpyAsync(part.data(), w->partials, sizeof(double) * part.size(), cudaMemcpyDeviceToHost,
-                                s));
-        TL_CUDA(cudaStreamSynchronize(s));
-        for (int b = 0; b < kGramBlocks; ++b)
-            for (int q = 0; q < kGramSums; ++q) S[q] += part[(size_t)b * kGramSums + q];
+        D.n = 0;
+        D.d[D.n++] = w->dnet;
+        for (int j = 0; j < w->nhist; ++j) D.d[D.n++] = w->hist[(w->cur - j + kHist) % kHist];
+        if ((rc = gram_project(c, w, D, &C, &gain))) return rc;
     }
     if ((rc = chunk_sync_scalars(c))) return rc;
     const double rr0 = c->sc_host->sum[0];
     *r0 = sqrt(fabs(rr0));
     *rr = rr0;
-    Coefs C;
-    for (int a = 0; a < kMaxDirs; ++a) C.c[a] = 0.0;
-    const double gain = D.n > 0 ? project(S, D.n, C.c) : 0.0;
     if (!(gain > 0.0)) return TL_OK;  // the plain start: u = u^n, r = r0
     k_combine<<<1216, 256, 0, s>>>(c->g, c->u0, D, C, c->u);
     if ((rc = launched(c, "warm start combine"))) return rc;
@@ -547,11 +578,13 @@ int warm_features(Chunk *c, float *dst) {
     }
     cudaStream_t s = c->stream;
     int rc;
-    k_resid0<<<1216, 256, 0, s>>>(c->g, c->u0, c->diag, c->kx, c->ky, w->r0);
+    // the history start of this step and its residual: the network learns
+    // the correction of u_h
+    k_resid_of<<<1216, 256, 0, s>>>(c->g, c->u0, w->ustart, c->diag, c->kx, c->ky, w->rh);
     if ((rc = launched(c, "residual launch"))) return rc;
     if ((rc = scales(c, w))) return rc;
-    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->r0, w->hist[w->cur], c->density, c->kx, c->ky,
-                                    w->scale, c->dt, nullptr, 0, dst);
+    k_features<<<1216, 256, 0, s>>>(c->g, c->u0, c->u, w->ustart, w->rh, w->hist[w->cur], c->density, c->kx,
+                                    c->ky, w->scale, c->dt, nullptr, 0, dst);
     if ((rc = launched(c, "features launch"))) return rc;
     TL_CUDA(cudaStreamSynchronize(s));
     return TL_OK;

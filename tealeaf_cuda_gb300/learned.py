@@ -3,10 +3,11 @@ the trainer of the residual network on the project's own BF16 tensor-core
 kernels (tl_nn_* in csrc/tl_conv.cu), model files, and the evaluation of
 what the warm starts save over the plain start.
 
-Network (tl_warm.cu): inputs (u^n / max|u^n|, log density, log1p Kx,
-log1p Ky, 100 dt, r0 / max|r0|, d_1 / max|r0|) with r0 = u^n - A u^n and
+Network (tl_warm.cu): it corrects the start that the last increments give
+alone, u_h; inputs (u^n / max|u^n|, log density, log1p Kx, log1p Ky,
+100 dt, r_h / max|r_h|, d_1 / max|r_h|) with r_h = u^n - A u_h and
 d_1 = u^n - u^{n-1}; six 3x3 convolutions of 32 channels (GELU, four
-residual blocks); output (u^{n+1} - u^n) / max|r0|.  The solve starts from
+residual blocks); output (u^{n+1} - u_h) / max|r_h|.  The solve starts from
 u^n plus the energy-minimising combination of the network's output and the
 last four increments, and keeps tl_eps * (plain start residual) as its exit
 test.  Torch only allocates
@@ -130,9 +131,9 @@ def load_model(path):
 # ----------------------------------------------------------------- data
 
 def trajectories(seeds, n, steps, device="cuda:0", precond="jac_diag"):
-    """Solve `steps` timesteps of each seeded deck (FP64, previous-step warm
-    start, which tracks u^{n-1}) and keep, per step, [n][n][NFEAT] = (network
-    inputs of step n, (u^{n+1} - u^n) / max|r0|)."""
+    """Solve `steps` timesteps of each seeded deck (FP64, increment-history
+    warm start, which tracks the increments) and keep, per step,
+    [n][n][NFEAT] = (network inputs of step n, (u^{n+1} - u_h) / max|r_h|)."""
     import torch
     lib = load()
     data = torch.empty((len(seeds) * steps, n, n, NFEAT), dtype=torch.float32, device=device)
