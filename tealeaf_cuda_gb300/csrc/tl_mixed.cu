@@ -280,23 +280,45 @@ __global__ void __launch_bounds__(kBlockThreads) k_v_w(GeoV g, const float *__re
         const int64_t P = g.pitch;
         int64_t i = (int64_t)(c + g.h) + (int64_t)(j0 + g.h) * P;
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 xm = live ? ld4(p, i - P) : z4;
-        float4 x0 = live ? ld4(p, i) : z4;
-        float4 ky0 = live ? ld4(ky, i) : z4;
+        // software pipeline, two rows deep: while row rr is computed, the p
+        // and Ky rows rr+2 and the Kx row rr+1 (with the lanes' edge values)
+        // are in flight.  A row is loaded only when it exists: padded rows
+        // run to ny + h, so row ny (the halo) is the last one read.
+        auto ldrow = [&](const float *f, int64_t at, int row) { return (live && row <= g.ny) ? ld4(f, at) : z4; };
+        float4 xm = ldrow(p, i - P, j0 - 1);
+        float4 x0 = ldrow(p, i, j0);
+        float4 xp = ldrow(p, i + P, j0 + 1);
+        float4 ky0 = ldrow(ky, i, j0);
+        float4 ky1 = ldrow(ky, i + P, j0 + 1);
+        float4 kxv = ldrow(kx, i, j0);
+        float kxe_edge = 0.f, xe_edge = 0.f, xw_edge = 0.f;  // the last / first lane's neighbours
+        if (lane == 31 && live) {
+            kxe_edge = kx[i + 4];
+            xe_edge = p[i + 4];
+        }
+        if (lane == 0 && live) xw_edge = p[i - 1];
 #pragma unroll
         for (int rr = 0; rr < kVRows; ++rr) {
             if (j0 + rr >= g.ny) break;
-            const float4 xp = live ? ld4(p, i + P) : z4;
-            const float4 ky1 = live ? ld4(ky, i + P) : z4;
-            const float4 kxv = live ? ld4(kx, i) : z4;
+            const int64_t in = i + P, inn = i + 2 * P;
+            const int rn = j0 + rr + 1, rnn = j0 + rr + 2;
+            const float4 xpp = ldrow(p, inn, rnn);
+            const float4 ky2 = ldrow(ky, inn, rnn);
+            const float4 kxn = ldrow(kx, in, rn);
+            float kxe_n = 0.f, xe_n = 0.f, xw_n = 0.f;
+            if (lane == 31 && live && rn <= g.ny) {
+                kxe_n = kx[in + 4];
+                xe_n = p[in + 4];
+            }
+            if (lane == 0 && live && rn <= g.ny) xw_n = p[in - 1];
             float kxe = __shfl_down_sync(0xffffffffu, kxv.x, 1);
             float xe = __shfl_down_sync(0xffffffffu, x0.x, 1);
             float xw = __shfl_up_sync(0xffffffffu, x0.w, 1);
             if (lane == 31 && live) {
-                kxe = kx[i + 4];
-                xe = p[i + 4];
+                kxe = kxe_edge;
+                xe = xe_edge;
             }
-            if (lane == 0 && live) xw = p[i - 1];
+            if (lane == 0 && live) xw = xw_edge;
             float4 o;
             o.x = cell_apply(x0.x, xp.x, xm.x, xw, x0.y, ky1.x, ky0.x, kxv.y, kxv.x);
             o.y = cell_apply(x0.y, xp.y, xm.y, x0.x, x0.z, ky1.y, ky0.y, kxv.z, kxv.y);
@@ -311,7 +333,13 @@ __global__ void __launch_bounds__(kBlockThreads) k_v_w(GeoV g, const float *__re
             }
             xm = x0;
             x0 = xp;
+            xp = xpp;
             ky0 = ky1;
+            ky1 = ky2;
+            kxv = kxn;
+            kxe_edge = kxe_n;
+            xe_edge = xe_n;
+            xw_edge = xw_n;
             i += P;
         }
     }
