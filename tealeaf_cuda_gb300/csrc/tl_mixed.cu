@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <chrono>
+#include <type_traits>
 
 #include "tl_internal.cuh"
 #include "tl_device.cuh"
@@ -663,7 +664,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 //
 // T inner steps per pass over HBM (the matrix-powers idea of the
 // reference's halo_depth > 1 PPCG, tea_leaf_ppcg.f90:199-221, done inside one
-// chunk).  A CTA owns a band of kFusedThreads columns (one column per
+// chunk).  A CTA owns a band of fused_threads<T>() columns (one column per
 // thread, T columns of halo on each side, recomputed) and a segment of
 // `seg` 4-row strips, and streams down the strips as a pipeline: at
 // iteration s, level 0 takes strip s (sd, rtemp, utemp and the strip's
@@ -673,15 +674,35 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 // thread's registers; horizontal ones go through shared memory (a buffer
 // per level and iteration parity), and so do the coefficients (a ring of the
 // T+1 strips in flight), so a coefficient is read from HBM once per pass and
-// the levels never wait on global loads: one barrier per strip.  Level T
+// the levels never wait on global loads: one barrier per strip.  Shared
+// memory keeps a column's strip as one float4 (its 4 rows) per array, so a
+// level reads its coefficients, its west and east neighbours' sd and the
+// east neighbour's Kx with one 16-byte load each.  Level T
 // stores its strip when it lies in the CTA's band and segment.  sd and rtemp
 // are read in halos that other CTAs own, so they ping-pong between launches;
 // utemp is read and written only at owned cells (its halo values are never
 // stored) and is updated in place.  Every value is computed with the
 // operations of k_pp_step in the same order, so T fused steps give the bits
 // of T single steps.
-constexpr int kFusedThreads = 224;  // 7 warps: two CTAs' shared memory fit an SM at T = 4
 constexpr int kFusedMax = 4;       // most steps fused into one pass
+constexpr int kFusedPrefetch = 1;  // strips beyond the next one that are prefetched into L2
+
+// CTA width (threads = columns) of a T-step pass.  Two CTAs run on an SM;
+// an SM sub-partition holds 16 K registers, so 7-warp CTAs get 128
+// registers a thread and 6-warp CTAs 168 (T >= 3 needs more than 128).
+template <int T>
+__host__ __device__ constexpr int fused_threads() {
+    return T >= 3 ? 192 : 224;
+}
+constexpr int kFusedThreadsMax = 224;
+constexpr int kFusedBandMin = 192 - 2 * kFusedMax;  // the narrowest band of any pass
+
+// the columns a T-step pass's CTA owns (the rest is halo)
+inline int fused_band(int T) {
+    const int nt = T >= 4 ? fused_threads<4>() : T == 3 ? fused_threads<3>() : T == 2 ? fused_threads<2>()
+                                                                                         : fused_threads<1>();
+    return nt - 2 * T;
+}
 
 struct PpFusedArgs {
     int nx, ny, h, pitch, pitch64, seg, band;
@@ -704,8 +725,8 @@ struct PpFusedArgs {
 // path's ppcg_rrn epilogue does: rrn, beta = rrn / rro, error = rro = rrn.
 // Every thread of the CTA calls it.
 __device__ void fused_rrn_reduce(double acc, double *partials, unsigned int *counter, DevScalars *sc) {
-    constexpr int NW = kFusedThreads / 32;
-    __shared__ double sh[NW];
+    __shared__ double sh[kFusedThreadsMax / 32];
+    const int NW = blockDim.x >> 5;
     __shared__ int is_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -742,33 +763,37 @@ __device__ void fused_rrn_reduce(double acc, double *partials, unsigned int *cou
     }
 }
 
-// coefficient arrays staged per strip: Kx, Ky, then cp, bfp (block) or Mi (diag),
-// packed per cell as one float4 {Kx, Ky, cp | Mi, bfp}
+// coefficient arrays staged per strip: Kx, Ky, then cp, bfp (block) or Mi (diag)
 template <int PC>
 __host__ __device__ constexpr int fused_narr() {
     return PC == TL_PREC_JAC_BLOCK ? 4 : (PC == TL_PREC_JAC_DIAG ? 3 : 2);
 }
 
-// shared-memory rows hold one value per thread plus a zero at each end, so
-// the west / east neighbours of the band's edge threads read zeros
-constexpr int kFusedRow = kFusedThreads + 2;
-
+// shared memory holds, per strip and array, one float4 per column: the
+// strip's 4 rows.  A row of columns has one entry per thread plus a zero
+// at each end, so the west / east neighbours of the band's edge threads
+// read zeros.
 template <int T, int PC>
 __host__ __device__ constexpr size_t fused_smem() {
-    return sizeof(float4) * kFusedRow * 4 * (T + 1) + sizeof(float) * kFusedRow * 4 * 2 * T;
+    return sizeof(float4) * (fused_threads<T>() + 2) * (fused_narr<PC>() * (T + 1) + 2 * T);
+}
+
+// row k (0..3, known at compile time) of a column's strip
+__device__ __forceinline__ float row_of(const float4 &v, int k) {
+    return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
 template <int T, int PC, bool LAST>
-__global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, DevScalars *sc) {
+__global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs a, DevScalars *sc) {
     if (*(volatile const int *)&sc->done) return;
-    constexpr int NT = kFusedThreads;
-    constexpr int SR = kFusedRow;  // shared-memory row stride
+    constexpr int NT = fused_threads<T>();
+    constexpr int SR = NT + 2;  // shared-memory row stride
     constexpr int NA = fused_narr<PC>();
     constexpr int R = T + 1;  // ring slots
     extern __shared__ float4 smem4[];
     const int tid = threadIdx.x;
-    float4 *const cfb = smem4 + 1;            // [R][4][SR]: coefficients by strip slot
-    float *const xsb = reinterpret_cast<float *>(smem4 + R * 4 * SR) + 1;  // [T][2][4][SR]: sd rows
+    float4 *const cfb = smem4 + 1;                // [R][NA][SR]: coefficients by strip slot
+    float4 *const xsb = smem4 + R * NA * SR + 1;  // [T][2][SR]: sd by producer level and parity
     const int col = blockIdx.x * a.band - T + tid;
     const bool incol = col >= 0 && col < a.nx;
     const bool own = incol && tid >= T && tid < T + a.band;
@@ -781,10 +806,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
         al[t] = (float)a.alphas[a.step0 + t - 1];
         be[t] = (float)a.betas[a.step0 + t - 1];
     }
-    {
-        float *z = reinterpret_cast<float *>(smem4);
-        for (int k = tid; k < (16 * R + 8 * T) * SR; k += NT) z[k] = 0.f;
-    }
+    for (int k = tid; k < (R * NA + 2 * T) * SR; k += NT) smem4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     // per producer level l < T: its output strip of the previous iteration
     // (sd, rtemp, utemp) and the last sd row of the one before
     float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
@@ -816,61 +838,72 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
             }
         }
     };
-    auto slot_of = [](int q) { return (q + 8 * R) % R; };  // q >= -2T >= -8
+    // L2 prefetch of the strip kFusedPrefetch after the next one, so that
+    // level 0's loads find it in L2: lane l < 4 (NA + 3) of each warp takes
+    // array l / 4 and row l % 4 and touches the lines of the warp's first
+    // and last columns (clamped to the field)
+    const int lane = tid & 31;
+    const int wc0 = max(col - lane, 0), wc1 = min(col - lane + 31, a.nx - 1);
+    const int pf_arr = lane >> 2, pf_k = lane & 3;
+    const float *const pf_base = pf_arr == 0   ? a.sd_in
+                                 : pf_arr == 1 ? a.rt_in
+                                 : pf_arr == 2 ? a.utemp
+                                 : pf_arr == 3 ? a.kx
+                                 : pf_arr == 4 ? a.ky
+                                 : pf_arr == 5 ? (PC == TL_PREC_JAC_BLOCK ? a.cp : a.mi)
+                                               : a.bfp;
+    const bool pf_on = pf_arr < NA + 3 && wc0 <= wc1;
+    auto prefetch = [&](int s2) {
+        const int row = 4 * s2 + pf_k;
+        if (pf_on && s2 >= 0 && row < a.ny) {
+            const float *p = pf_base + (row + a.h) * a.pitch + a.h;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc0));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc1));
+        }
+    };
     load(sb - T);
+#pragma unroll
+    for (int d = 1; d <= kFusedPrefetch; ++d) prefetch(sb - T + d);
+    int slot = (sb - T + 8 * R) % R;  // ring slot of strip s (sb - T >= -2T >= -8)
     double racc = 0.0;  // LAST with rrn: this thread's (r - r_store).z
     __syncthreads();
     for (int s = sb - T; s < se + T; ++s) {
         float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
         {
-            float4 *cf = cfb + slot_of(s) * 4 * SR + tid;
+            float4 *cf = cfb + slot * NA * SR + tid;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 cS[k] = ldS[k];
                 cR[k] = ldR[k];
                 cU[k] = ldU[k];
-                xsb[((0 * 2 + (s & 1)) * 4 + k) * SR + tid] = ldS[k];
-                cf[k * SR] = make_float4(ldC[0][k], ldC[1][k], NA > 2 ? ldC[NA > 2 ? 2 : 0][k] : 0.f,
-                                         NA > 3 ? ldC[NA > 3 ? 3 : 0][k] : 0.f);
             }
+            xsb[(s & 1) * SR + tid] = make_float4(ldS[0], ldS[1], ldS[2], ldS[3]);
+#pragma unroll
+            for (int q = 0; q < NA; ++q) cf[q * SR] = make_float4(ldC[q][0], ldC[q][1], ldC[q][2], ldC[q][3]);
         }
         if (s + 1 < se + T) load(s + 1);
+        if (s + 1 + kFusedPrefetch < se + T) prefetch(s + 1 + kFusedPrefetch);
+        // levels 1..T; FULL: every level's strip lies in the field and has 4
+        // rows, so no level tests rows (columns outside the field compute on
+        // the zeros they loaded and are never stored) and the levels form one
+        // block of straight-line code
+        auto levels = [&](auto full) {
+            constexpr bool FULL = decltype(full)::value;
 #pragma unroll
         for (int t = 1; t <= T; ++t) {
             const int q = s - t;
-            const int m = (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
-            const float4 *cf = cfb + slot_of(q) * 4 * SR + tid;       // this strip
-            const float4 *cn = cfb + slot_of(q + 1) * 4 * SR + tid;   // the strip above it
-            const float *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * 4 * SR + tid;
+            const int m = FULL ? 4 : (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
+            const int sq = slot - t < 0 ? slot - t + R : slot - t;  // ring slot of strip q
+            const int sn = sq + 1 == R ? 0 : sq + 1;                  // and of strip q + 1
+            const float4 *cf = cfb + sq * NA * SR + tid;
+            const float4 *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * SR + tid;
             const float(&x0)[4] = sdP[t - 1];
             float oS[4], oR[4], oU[4];
-            // the strip's coefficient rows, one float4 each, and the east
-            // neighbours' Kx by shuffle (the last lane reads its neighbour's
-            // row): read once per level by every lane, before the row tests,
-            // so that no single float is read out of the packed rows
-            // (T = 4 has no registers to spare for this: it reads the rows
-            // where it uses them)
-            constexpr bool PRE = T <= 3;
-            float4 c4[4];
-            float kxe4[4], ky_top = 0.f;
-            if constexpr (PRE) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) c4[k] = cf[k * SR];
-                ky_top = cn[0].y;  // the face above the strip's last row
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    kxe4[k] = __shfl_down_sync(0xffffffffu, c4[k].x, 1);
-                    if ((tid & 31) == 31) kxe4[k] = cf[k * SR + 1].x;
-                }
-            }
-            auto row = [&](int k) -> float4 {
-                if constexpr (PRE) return c4[k];
-                else return cf[k * SR];
-            };
-            auto east_kx = [&](int k) -> float {
-                if constexpr (PRE) return kxe4[k];
-                else return cf[k * SR + 1].x;
-            };
+            // the strip's coefficients, its west / east neighbours' sd and the
+            // east neighbour's Kx: one float4 (4 rows) each
+            const float4 kx4 = cf[0], ky4 = cf[SR], kxe4 = cf[1];
+            const float ky_top = cfb[sn * NA * SR + SR + tid].x;  // the face above row 3
+            const float4 xw4 = xp[-1], xe4 = xp[1];
             // one inner step on the strip's first mm rows (mm == 4: no row tests)
             auto step = [&](const int mm) {
                 float z[4];
@@ -881,29 +914,34 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
                         const float c = x0[k];
                         const float n = k < 3 ? x0[k + 1] : cS[0];
                         const float sv = k > 0 ? x0[k - 1] : sdL[t - 1];
-                        const float4 cc = row(k);
-                        const float kyn = k < 3 ? row(k < 3 ? k + 1 : 3).y : (PRE ? ky_top : cn[0].y);
-                        oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, xp[k * SR - 1], xp[k * SR + 1], kyn, cc.y,
-                                                           east_kx(k), cc.x);
+                        const float kyn = k < 3 ? row_of(ky4, k + 1) : ky_top;
+                        oR[k] = rtP[t - 1][k] - cell_apply(c, n, sv, row_of(xw4, k), row_of(xe4, k), kyn,
+                                                           row_of(ky4, k), row_of(kxe4, k), row_of(kx4, k));
                     }
                 }
                 if constexpr (PC == TL_PREC_JAC_BLOCK) {
                     // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
                     // z_k = dp_k - cp_k z_{k+1}
+                    const float4 bf4 = cf[3 * SR];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        if (k < mm) {
-                            const float4 cc = row(k);
-                            z[k] = k == 0 ? oR[0] * cc.w : fmaf(cc.y, z[k - 1], oR[k]) * cc.w;
-                        }
+                        if (k < mm)
+                            z[k] = k == 0 ? oR[0] * row_of(bf4, 0)
+                                          : fmaf(row_of(ky4, k), z[k > 0 ? k - 1 : 0], oR[k]) * row_of(bf4, k);
                     }
+                    const float4 cp4 = cf[2 * SR];
 #pragma unroll
                     for (int k = 2; k >= 0; --k)
-                        if (k < mm - 1) z[k] = fmaf(-row(k).z, z[k + 1], z[k]);
+                        if (k < mm - 1) z[k] = fmaf(-row_of(cp4, k), z[k + 1], z[k]);
+                } else if constexpr (PC == TL_PREC_JAC_DIAG) {
+                    const float4 mi4 = cf[2 * SR];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < mm) z[k] = oR[k] * row_of(mi4, k);
                 } else {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        if (k < mm) z[k] = PC == TL_PREC_JAC_DIAG ? oR[k] * row(k).z : oR[k];
+                        if (k < mm) z[k] = oR[k];
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
@@ -913,7 +951,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
                     }
                 }
             };
-            if (m == 4) step(4);
+            if (FULL || m == 4) step(4);
             else step(m);
             // level t-1 has been consumed: its output of this iteration moves in
             sdL[t - 1] = sdP[t - 1][3];
@@ -927,8 +965,7 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
                 cU[k] = oU[k];
             }
             if (t < T) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) xsb[((t * 2 + (s & 1)) * 4 + k) * SR + tid] = oS[k];
+                xsb[(t * 2 + (s & 1)) * SR + tid] = make_float4(oS[0], oS[1], oS[2], oS[3]);
             } else if (own && q >= sb && q < se) {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
@@ -949,6 +986,10 @@ __global__ void __launch_bounds__(kFusedThreads, 2) k_pp_fused(PpFusedArgs a, De
                 }
             }
         }
+        };
+        if (s - T >= 0 && 4 * s <= a.ny) levels(std::true_type{});
+        else levels(std::false_type{});
+        slot = slot + 1 == R ? 0 : slot + 1;
         __syncthreads();
     }
     if (LAST && a.rrn) fused_rrn_reduce(racc, a.partials, a.counter, sc);
@@ -1146,8 +1187,7 @@ int mixed_alloc(Chunk *c) {
     mx->counter = (unsigned int *)p;
     mx->partials = (double *)((char *)p + 256);
     // the most CTAs a fused pass can have: the narrowest band, one strip per segment
-    const size_t fcta = (size_t)((c->nx + kFusedThreads - 2 * kFusedMax - 1) / (kFusedThreads - 2 * kFusedMax)) *
-                        (size_t)((c->ny + 3) / 4);
+    const size_t fcta = (size_t)((c->nx + kFusedBandMin - 1) / kFusedBandMin) * (size_t)((c->ny + 3) / 4);
     e = cudaMalloc(&p, sizeof(double) * fcta);
     if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");
     mx->allocs.push_back(p);
@@ -1245,7 +1285,7 @@ void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, DevScalars *
         cudaFuncSetAttribute(k_pp_fused<T, PC, LAST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         configured = true;
     }
-    k_pp_fused<T, PC, LAST><<<grid, kFusedThreads, bytes, s>>>(a, sc);
+    k_pp_fused<T, PC, LAST><<<grid, fused_threads<T>(), bytes, s>>>(a, sc);
 }
 
 template <int T, int PC>
@@ -1297,7 +1337,7 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
             a.h = c->h;
             a.pitch = c->pitch;
             a.pitch64 = c->pitch;
-            a.band = kFusedThreads - 2 * T;
+            a.band = fused_band(T);
             a.seg = c->inner_seg;
             if (a.seg < 1) {
                 // automatic: one wave of 2 CTAs per SM with the longest segments
