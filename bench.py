@@ -105,6 +105,10 @@ TRAFFIC_PER_CELL = {
 }
 
 
+INNER_STEPS = 10  # tl_ppcg_inner_steps of the workload's deck
+FUSED_STEPS = 5   # FP32 inner steps per fused pass (the library's default)
+
+
 def bytes_per_cell(kernel, precond):
     """algorithmic bytes per cell of `kernel` under preconditioner `precond`"""
     if kernel == "mixed_pp_step":
@@ -131,8 +135,12 @@ def bytes_per_cell(kernel, precond):
         # bfp); write u, r (FP64) and rtemp, sd, utemp (FP32)
         return {"none": 60, "jac_diag": 64, "jac_block": 72}[precond]
     if kernel == "mixed_pp_fused":
-        # the same arrays once per pass of several inner steps
-        return {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
+        # the same arrays once per pass of several inner steps; the last pass
+        # of a solve writes z (FP64) instead of sd, rtemp and utemp (FP32):
+        # the mean over the INNER_STEPS / FUSED_STEPS passes of one solve
+        passes = -(-INNER_STEPS // FUSED_STEPS)
+        full = {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
+        return full - 4.0 / passes
     return BYTES_PER_CELL.get(kernel)
 
 
@@ -142,7 +150,7 @@ def make_deck(n, solver="cg", precond="jac_diag", max_iters=10000, end_step=1000
             f"x_cells={n}\ny_cells={n}\nxmin=0.0\nymin=0.0\nxmax=10.0\nymax=10.0\n"
             f"initial_timestep=0.004\nend_step={end_step}\ntl_max_iters={max_iters}\n"
             f"tl_use_{solver}\ntl_preconditioner_type {precond}\ntl_eps 1.0e-15\n"
-            f"tl_ppcg_inner_steps 10\ntl_precision {precision}\ntl_warm_start {warm}\n"
+            f"tl_ppcg_inner_steps {INNER_STEPS}\ntl_precision {precision}\ntl_warm_start {warm}\n"
             f"summary_frequency 0\n*endtea\n")
 
 

@@ -181,7 +181,7 @@ void *tl_chunk_stream(tl_chunk_t *ch);
  * (TL_ERR_ARG past the last name) */
 int tl_set_profiling(tl_chunk_t *ch, int on);
 int tl_profile_reset(tl_chunk_t *ch);
-/* mixed-precision PPCG: run `steps` (1..4) FP32 inner steps per pass over
+/* mixed-precision PPCG: run `steps` (1..5) FP32 inner steps per pass over
  * HBM (temporal blocking; 1 = one kernel per inner step), each CTA taking
  * `seg_strips` 4-row strips of a column band (0: chosen from the grid size,
  * one wave of CTAs).  The inner steps give the same bits for every setting.
@@ -189,7 +189,7 @@ int tl_profile_reset(tl_chunk_t *ch);
  * saving a pass over r, r_store and z; that sum then runs in the fused
  * grid's order, so solves with different settings agree to round-off rather
  * than bit for bit (and on GB300 the fold is slower: it adds FP64 work to
- * an issue-bound pass).  Default 4, 0, 0. */
+ * an issue-bound pass).  Default 5, 0, 0. */
 int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips, int fold_rrn);
 int tl_profile_read(tl_chunk_t *ch, int idx, const char **name, long long *launches, double *ms);
 /* the process-wide chunk the reference-named entry points act on */

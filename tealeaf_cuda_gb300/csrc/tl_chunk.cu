@@ -524,8 +524,9 @@ int tl_set_inner_fusion(tl_chunk_t *ch, int steps, int seg_strips, int fold_rrn)
         set_error("tl_set_inner_fusion: no chunk");
         return TL_ERR_STATE;
     }
-    if (steps < 1 || steps > 4 || seg_strips < 0) {
-        set_error("tl_set_inner_fusion: steps must be 1..4 and seg_strips >= 0 (got %d, %d)", steps, seg_strips);
+    if (steps < 1 || steps > kFusedMax || seg_strips < 0) {
+        set_error("tl_set_inner_fusion: steps must be 1..%d and seg_strips >= 0 (got %d, %d)", kFusedMax, steps,
+                  seg_strips);
         return TL_ERR_ARG;
     }
     Chunk *c = ch->c;

@@ -231,7 +231,8 @@ int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
 // tells whether the last pass also summed (r - r_store).z (kEpiPpcgRrn)
 int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn);
 void drop_graphs(Chunk *c);        // after a change that captured graphs depend on
-constexpr int kInnerFuseDefault = 4;
+constexpr int kFusedMax = 5;           // most FP32 PPCG inner steps fused into one pass
+constexpr int kInnerFuseDefault = 5;
 constexpr int kInnerSegDefault = 0;
 // warm starts (tl_warm.cu)
 void warm_free(Chunk *c);

@@ -684,7 +684,6 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 // stored) and is updated in place.  Every value is computed with the
 // operations of k_pp_step in the same order, so T fused steps give the bits
 // of T single steps.
-constexpr int kFusedMax = 4;       // most steps fused into one pass
 constexpr int kFusedPrefetch = 1;  // strips beyond the next one that are prefetched into L2
 
 // CTA width (threads = columns) of a T-step pass.  Two CTAs run on an SM;
@@ -699,13 +698,19 @@ constexpr int kFusedBandMin = 192 - 2 * kFusedMax;  // the narrowest band of any
 
 // the columns a T-step pass's CTA owns (the rest is halo)
 inline int fused_band(int T) {
-    const int nt = T >= 4 ? fused_threads<4>() : T == 3 ? fused_threads<3>() : T == 2 ? fused_threads<2>()
-                                                                                         : fused_threads<1>();
+    const int nt = T >= 5   ? fused_threads<5>()
+                   : T == 4 ? fused_threads<4>()
+                   : T == 3 ? fused_threads<3>()
+                   : T == 2 ? fused_threads<2>()
+                            : fused_threads<1>();
     return nt - 2 * T;
 }
 
 struct PpFusedArgs {
-    int nx, ny, h, pitch, pitch64, seg, band;
+    int nx, ny, h, pitch, pitch64;
+    int band;    // columns a CTA owns (fused_band(T))
+    int nbands;  // bands across the field
+    int chunk;   // strips a CTA takes from the band-major (band, strip) sequence
     const float *sd_in, *rt_in;
     float *sd_out, *rt_out, *utemp;
     const float *kx, *ky, *mi, *cp, *bfp;
@@ -794,12 +799,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
     const int tid = threadIdx.x;
     float4 *const cfb = smem4 + 1;                // [R][NA][SR]: coefficients by strip slot
     float4 *const xsb = smem4 + R * NA * SR + 1;  // [T][2][SR]: sd by producer level and parity
-    const int col = blockIdx.x * a.band - T + tid;
-    const bool incol = col >= 0 && col < a.nx;
-    const bool own = incol && tid >= T && tid < T + a.band;
     const int nstrips = (a.ny + 3) >> 2;
-    const int sb = blockIdx.y * a.seg;
-    const int se = min(sb + a.seg, nstrips);
     float al[T], be[T];
 #pragma unroll
     for (int t = 0; t < T; ++t) {
@@ -807,214 +807,229 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
         be[t] = (float)a.betas[a.step0 + t - 1];
     }
     for (int k = tid; k < (R * NA + 2 * T) * SR; k += NT) smem4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    // the pipeline registers carried from one strip to the next: per
-    // producer level l < T its output strip of the previous iteration (sd,
-    // rtemp, utemp) and the last sd row of the one before, and level 0's
-    // loads of the next strip.  For T <= 3 the strip loop is unrolled by two
-    // with two sets that swap roles, so nothing is copied from one set to the
-    // other.
-    struct Pipe {
-        float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
-        float ldS[4], ldR[4], ldU[4], ldC[NA][4];
-    };
-    Pipe pa, pb;
-#pragma unroll
-    for (int l = 0; l < T; ++l) {
-        pa.sdL[l] = 0.f;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) pa.sdP[l][k] = pa.rtP[l][k] = pa.utP[l][k] = 0.f;
-    }
-    // level 0 loads, one strip ahead (32-bit offsets: a field has < 2^31 elements)
-    const int cbase = col + a.h;
-    auto load = [&](int s, Pipe &o) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int row = 4 * s + k;
-            const bool v = incol && s >= 0 && row < a.ny;
-            const int i = cbase + (row + a.h) * a.pitch;
-            o.ldS[k] = v ? a.sd_in[i] : 0.f;
-            o.ldR[k] = v ? a.rt_in[i] : 0.f;
-            o.ldU[k] = v ? a.utemp[i] : 0.f;
-            o.ldC[0][k] = v ? __ldg(&a.kx[i]) : 0.f;
-            o.ldC[1][k] = v ? __ldg(&a.ky[i]) : 0.f;
-            if (PC == TL_PREC_JAC_BLOCK) {
-                o.ldC[2][k] = v ? __ldg(&a.cp[i]) : 0.f;
-                o.ldC[3][k] = v ? __ldg(&a.bfp[i]) : 0.f;
-            } else if (PC == TL_PREC_JAC_DIAG) {
-                o.ldC[NA - 1][k] = v ? __ldg(&a.mi[i]) : 0.f;
-            }
-        }
-    };
-    // L2 prefetch of the strip kFusedPrefetch after the next one, so that
-    // level 0's loads find it in L2: lane l < 4 (NA + 3) of each warp takes
-    // array l / 4 and row l % 4 and touches the lines of the warp's first
-    // and last columns (clamped to the field)
-    const int lane = tid & 31;
-    const int wc0 = max(col - lane, 0), wc1 = min(col - lane + 31, a.nx - 1);
-    const int pf_arr = lane >> 2, pf_k = lane & 3;
-    const float *const pf_base = pf_arr == 0   ? a.sd_in
-                                 : pf_arr == 1 ? a.rt_in
-                                 : pf_arr == 2 ? a.utemp
-                                 : pf_arr == 3 ? a.kx
-                                 : pf_arr == 4 ? a.ky
-                                 : pf_arr == 5 ? (PC == TL_PREC_JAC_BLOCK ? a.cp : a.mi)
-                                               : a.bfp;
-    const bool pf_on = pf_arr < NA + 3 && wc0 <= wc1;
-    auto prefetch = [&](int s2) {
-        const int row = 4 * s2 + pf_k;
-        if (pf_on && s2 >= 0 && row < a.ny) {
-            const float *p = pf_base + (row + a.h) * a.pitch + a.h;
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc0));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc1));
-        }
-    };
-    load(sb - T, pa);
-#pragma unroll
-    for (int d = 1; d <= kFusedPrefetch; ++d) prefetch(sb - T + d);
-    int slot = (sb - T + 8 * R) % R;  // ring slot of strip s (sb - T >= -2T >= -8)
     double racc = 0.0;  // LAST with rrn: this thread's (r - r_store).z
-    const int s_end = se + T;
-    __syncthreads();
-    // one strip iteration: level 0 takes strip s from `in`, levels 1..T
-    // advance, and what the next iteration needs goes to `out`
-    auto iter = [&](const int s, const Pipe &in, Pipe &out) {
-        {
-            float4 *cf = cfb + slot * NA * SR + tid;
-            xsb[(s & 1) * SR + tid] = make_float4(in.ldS[0], in.ldS[1], in.ldS[2], in.ldS[3]);
+    // the CTA's share of the band-major sequence of (band, strip) pairs: a
+    // share that reaches the end of a band goes on at the top of the next
+    // one with a new pipeline (what a pipeline holds before its first strip
+    // never reaches a stored value)
+    // (32-bit: a field has fewer than 2^31 cells, so fewer (band, strip) pairs)
+    const int w_end = min((int)(blockIdx.x + 1) * a.chunk, a.nbands * nstrips);
+    for (int w = (int)blockIdx.x * a.chunk; w < w_end;) {
+        const int band = w / nstrips;
+        const int sb = w - band * nstrips;
+        const int se = min(nstrips, sb + (w_end - w));
+        w += se - sb;
+        const int col = band * a.band - T + tid;
+        const bool incol = col >= 0 && col < a.nx;
+        const bool own = incol && tid >= T && tid < T + a.band;
+        // the pipeline registers carried from one strip to the next: per
+        // producer level l < T its output strip of the previous iteration
+        // (sd, rtemp, utemp) and the last sd row of the one before, and
+        // level 0's loads of the next strip.  For T <= 3 the strip loop is
+        // unrolled by two with two sets that swap roles, so nothing is
+        // copied from one set to the other.
+        struct Pipe {
+            float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
+            float ldS[4], ldR[4], ldU[4], ldC[NA][4];
+        };
+        Pipe pa, pb;
 #pragma unroll
-            for (int q = 0; q < NA; ++q)
-                cf[q * SR] = make_float4(in.ldC[q][0], in.ldC[q][1], in.ldC[q][2], in.ldC[q][3]);
+        for (int l = 0; l < T; ++l) {
+            pa.sdL[l] = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) pa.sdP[l][k] = pa.rtP[l][k] = pa.utP[l][k] = 0.f;
         }
-        if (s + 1 < s_end) load(s + 1, out);
-        if (s + 1 + kFusedPrefetch < s_end) prefetch(s + 1 + kFusedPrefetch);
-        // levels 1..T; FULL: every level's strip lies in the field and has 4
-        // rows, so no level tests rows (columns outside the field compute on
-        // the zeros they loaded and are never stored) and the levels form one
-        // block of straight-line code
-        auto levels = [&](auto full) {
-            constexpr bool FULL = decltype(full)::value;
-            float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
+        // level 0 loads, one strip ahead (32-bit offsets: a field has < 2^31 elements)
+        const int cbase = col + a.h;
+        auto load = [&](int s, Pipe &o) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                cS[k] = in.ldS[k];
-                cR[k] = in.ldR[k];
-                cU[k] = in.ldU[k];
+                const int row = 4 * s + k;
+                const bool v = incol && s >= 0 && row < a.ny;
+                const int i = cbase + (row + a.h) * a.pitch;
+                o.ldS[k] = v ? a.sd_in[i] : 0.f;
+                o.ldR[k] = v ? a.rt_in[i] : 0.f;
+                o.ldU[k] = v ? a.utemp[i] : 0.f;
+                o.ldC[0][k] = v ? __ldg(&a.kx[i]) : 0.f;
+                o.ldC[1][k] = v ? __ldg(&a.ky[i]) : 0.f;
+                if (PC == TL_PREC_JAC_BLOCK) {
+                    o.ldC[2][k] = v ? __ldg(&a.cp[i]) : 0.f;
+                    o.ldC[3][k] = v ? __ldg(&a.bfp[i]) : 0.f;
+                } else if (PC == TL_PREC_JAC_DIAG) {
+                    o.ldC[NA - 1][k] = v ? __ldg(&a.mi[i]) : 0.f;
+                }
             }
+        };
+        // L2 prefetch of the strip kFusedPrefetch after the next one, so that
+        // level 0's loads find it in L2: lane l < 4 (NA + 3) of each warp takes
+        // array l / 4 and row l % 4 and touches the lines of the warp's first
+        // and last columns (clamped to the field)
+        const int lane = tid & 31;
+        const int wc0 = max(col - lane, 0), wc1 = min(col - lane + 31, a.nx - 1);
+        const int pf_arr = lane >> 2, pf_k = lane & 3;
+        const float *const pf_base = pf_arr == 0   ? a.sd_in
+                                     : pf_arr == 1 ? a.rt_in
+                                     : pf_arr == 2 ? a.utemp
+                                     : pf_arr == 3 ? a.kx
+                                     : pf_arr == 4 ? a.ky
+                                     : pf_arr == 5 ? (PC == TL_PREC_JAC_BLOCK ? a.cp : a.mi)
+                                                   : a.bfp;
+        const bool pf_on = pf_arr < NA + 3 && wc0 <= wc1;
+        auto prefetch = [&](int s2) {
+            const int row = 4 * s2 + pf_k;
+            if (pf_on && s2 >= 0 && row < a.ny) {
+                const float *p = pf_base + (row + a.h) * a.pitch + a.h;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc0));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc1));
+            }
+        };
+        load(sb - T, pa);
 #pragma unroll
-            for (int t = 1; t <= T; ++t) {
-                const int q = s - t;
-                const int m = FULL ? 4 : (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
-                const int sq = slot - t < 0 ? slot - t + R : slot - t;  // ring slot of strip q
-                const int sn = sq + 1 == R ? 0 : sq + 1;                  // and of strip q + 1
-                const float4 *cf = cfb + sq * NA * SR + tid;
-                const float4 *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * SR + tid;
-                const float(&x0)[4] = in.sdP[t - 1];
-                float oS[4], oR[4], oU[4];
-                // the strip's coefficients, its west / east neighbours' sd and the
-                // east neighbour's Kx: one float4 (4 rows) each
-                const float4 kx4 = cf[0], ky4 = cf[SR], kxe4 = cf[1];
-                const float ky_top = cfb[sn * NA * SR + SR + tid].x;  // the face above row 3
-                const float4 xw4 = xp[-1], xe4 = xp[1];
-                // one inner step on the strip's first mm rows (mm == 4: no row tests)
-                auto step = [&](const int mm) {
-                    float z[4];
+        for (int d = 1; d <= kFusedPrefetch; ++d) prefetch(sb - T + d);
+        int slot = (sb - T + 8 * R) % R;  // ring slot of strip s (sb - T >= -2T >= -8)
+        const int s_end = se + T;
+        __syncthreads();
+        // one strip iteration: level 0 takes strip s from `in`, levels 1..T
+        // advance, and what the next iteration needs goes to `out`
+        auto iter = [&](const int s, const Pipe &in, Pipe &out) {
+            {
+                float4 *cf = cfb + slot * NA * SR + tid;
+                xsb[(s & 1) * SR + tid] = make_float4(in.ldS[0], in.ldS[1], in.ldS[2], in.ldS[3]);
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        oS[k] = oR[k] = oU[k] = z[k] = 0.f;
-                        if (k < mm) {
-                            const float c = x0[k];
-                            const float n = k < 3 ? x0[k + 1] : cS[0];
-                            const float sv = k > 0 ? x0[k - 1] : in.sdL[t - 1];
-                            const float kyn = k < 3 ? row_of(ky4, k + 1) : ky_top;
-                            oR[k] = in.rtP[t - 1][k] - cell_apply(c, n, sv, row_of(xw4, k), row_of(xe4, k), kyn,
-                                                                  row_of(ky4, k), row_of(kxe4, k), row_of(kx4, k));
-                        }
-                    }
-                    if constexpr (PC == TL_PREC_JAC_BLOCK) {
-                        // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
-                        // z_k = dp_k - cp_k z_{k+1}
-                        const float4 bf4 = cf[3 * SR];
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            if (k < mm)
-                                z[k] = k == 0 ? oR[0] * row_of(bf4, 0)
-                                              : fmaf(row_of(ky4, k), z[k > 0 ? k - 1 : 0], oR[k]) * row_of(bf4, k);
-                        }
-                        const float4 cp4 = cf[2 * SR];
-#pragma unroll
-                        for (int k = 2; k >= 0; --k)
-                            if (k < mm - 1) z[k] = fmaf(-row_of(cp4, k), z[k + 1], z[k]);
-                    } else if constexpr (PC == TL_PREC_JAC_DIAG) {
-                        const float4 mi4 = cf[2 * SR];
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (k < mm) z[k] = oR[k] * row_of(mi4, k);
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (k < mm) z[k] = oR[k];
-                    }
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        if (k < mm) {
-                            oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
-                            oU[k] = in.utP[t - 1][k] + oS[k];
-                        }
-                    }
-                };
-                if (FULL || m == 4) step(4);
-                else step(m);
-                // level t-1's output of this iteration is what level t reads next time
-                out.sdL[t - 1] = x0[3];
+                for (int q = 0; q < NA; ++q)
+                    cf[q * SR] = make_float4(in.ldC[q][0], in.ldC[q][1], in.ldC[q][2], in.ldC[q][3]);
+            }
+            if (s + 1 < s_end) load(s + 1, out);
+            if (s + 1 + kFusedPrefetch < s_end) prefetch(s + 1 + kFusedPrefetch);
+            // levels 1..T; FULL: every level's strip lies in the field and has 4
+            // rows, so no level tests rows (columns outside the field compute on
+            // the zeros they loaded and are never stored) and the levels form one
+            // block of straight-line code
+            auto levels = [&](auto full) {
+                constexpr bool FULL = decltype(full)::value;
+                float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    out.sdP[t - 1][k] = cS[k];
-                    out.rtP[t - 1][k] = cR[k];
-                    out.utP[t - 1][k] = cU[k];
-                    cS[k] = oS[k];
-                    cR[k] = oR[k];
-                    cU[k] = oU[k];
+                    cS[k] = in.ldS[k];
+                    cR[k] = in.ldR[k];
+                    cU[k] = in.ldU[k];
                 }
-                if (t < T) {
-                    xsb[(t * 2 + (s & 1)) * SR + tid] = make_float4(oS[0], oS[1], oS[2], oS[3]);
-                } else if (own && q >= sb && q < se) {
+#pragma unroll
+                for (int t = 1; t <= T; ++t) {
+                    const int q = s - t;
+                    const int m = FULL ? 4 : (q >= 0 && q < nstrips && incol) ? min(4, a.ny - 4 * q) : 0;
+                    const int sq = slot - t < 0 ? slot - t + R : slot - t;  // ring slot of strip q
+                    const int sn = sq + 1 == R ? 0 : sq + 1;                  // and of strip q + 1
+                    const float4 *cf = cfb + sq * NA * SR + tid;
+                    const float4 *xp = xsb + ((t - 1) * 2 + ((s - 1) & 1)) * SR + tid;
+                    const float(&x0)[4] = in.sdP[t - 1];
+                    float oS[4], oR[4], oU[4];
+                    // the strip's coefficients, its west / east neighbours' sd and the
+                    // east neighbour's Kx: one float4 (4 rows) each
+                    const float4 kx4 = cf[0], ky4 = cf[SR], kxe4 = cf[1];
+                    const float ky_top = cfb[sn * NA * SR + SR + tid].x;  // the face above row 3
+                    const float4 xw4 = xp[-1], xe4 = xp[1];
+                    // one inner step on the strip's first mm rows (mm == 4: no row tests)
+                    auto step = [&](const int mm) {
+                        float z[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            oS[k] = oR[k] = oU[k] = z[k] = 0.f;
+                            if (k < mm) {
+                                const float c = x0[k];
+                                const float n = k < 3 ? x0[k + 1] : cS[0];
+                                const float sv = k > 0 ? x0[k - 1] : in.sdL[t - 1];
+                                const float kyn = k < 3 ? row_of(ky4, k + 1) : ky_top;
+                                oR[k] = in.rtP[t - 1][k] - cell_apply(c, n, sv, row_of(xw4, k), row_of(xe4, k), kyn,
+                                                                      row_of(ky4, k), row_of(kxe4, k), row_of(kx4, k));
+                            }
+                        }
+                        if constexpr (PC == TL_PREC_JAC_BLOCK) {
+                            // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
+                            // z_k = dp_k - cp_k z_{k+1}
+                            const float4 bf4 = cf[3 * SR];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k) {
+                                if (k < mm)
+                                    z[k] = k == 0 ? oR[0] * row_of(bf4, 0)
+                                                  : fmaf(row_of(ky4, k), z[k > 0 ? k - 1 : 0], oR[k]) * row_of(bf4, k);
+                            }
+                            const float4 cp4 = cf[2 * SR];
+#pragma unroll
+                            for (int k = 2; k >= 0; --k)
+                                if (k < mm - 1) z[k] = fmaf(-row_of(cp4, k), z[k + 1], z[k]);
+                        } else if constexpr (PC == TL_PREC_JAC_DIAG) {
+                            const float4 mi4 = cf[2 * SR];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                if (k < mm) z[k] = oR[k] * row_of(mi4, k);
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                if (k < mm) z[k] = oR[k];
+                        }
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            if (k < mm) {
+                                oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
+                                oU[k] = in.utP[t - 1][k] + oS[k];
+                            }
+                        }
+                    };
+                    if (FULL || m == 4) step(4);
+                    else step(m);
+                    // level t-1's output of this iteration is what level t reads next time
+                    out.sdL[t - 1] = x0[3];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        if (k < m) {
-                            const int row = 4 * q + k;
-                            if (LAST) {
-                                const int64_t i64 = (int64_t)cbase + (int64_t)(row + a.h) * a.pitch64;
-                                const double zv = (double)oU[k];
-                                a.z64[i64] = zv;
-                                if (a.rrn) racc = fma(a.r64[i64] - a.rs64[i64], zv, racc);
-                            } else {
-                                const int i = cbase + (row + a.h) * a.pitch;
-                                a.sd_out[i] = oS[k];
-                                a.rt_out[i] = oR[k];
-                                a.utemp[i] = oU[k];
+                        out.sdP[t - 1][k] = cS[k];
+                        out.rtP[t - 1][k] = cR[k];
+                        out.utP[t - 1][k] = cU[k];
+                        cS[k] = oS[k];
+                        cR[k] = oR[k];
+                        cU[k] = oU[k];
+                    }
+                    if (t < T) {
+                        xsb[(t * 2 + (s & 1)) * SR + tid] = make_float4(oS[0], oS[1], oS[2], oS[3]);
+                    } else if (own && q >= sb && q < se) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            if (k < m) {
+                                const int row = 4 * q + k;
+                                if (LAST) {
+                                    const int64_t i64 = (int64_t)cbase + (int64_t)(row + a.h) * a.pitch64;
+                                    const double zv = (double)oU[k];
+                                    a.z64[i64] = zv;
+                                    if (a.rrn) racc = fma(a.r64[i64] - a.rs64[i64], zv, racc);
+                                } else {
+                                    const int i = cbase + (row + a.h) * a.pitch;
+                                    a.sd_out[i] = oS[k];
+                                    a.rt_out[i] = oR[k];
+                                    a.utemp[i] = oU[k];
+                                }
                             }
                         }
                     }
                 }
-            }
+            };
+            if (s - T >= 0 && 4 * s <= a.ny) levels(std::true_type{});
+            else levels(std::false_type{});
+            slot = slot + 1 == R ? 0 : slot + 1;
+            __syncthreads();
         };
-        if (s - T >= 0 && 4 * s <= a.ny) levels(std::true_type{});
-        else levels(std::false_type{});
-        slot = slot + 1 == R ? 0 : slot + 1;
-        __syncthreads();
-    };
-    if constexpr (T <= 3) {
-        int s = sb - T;
-        for (; s + 1 < s_end; s += 2) {
-            iter(s, pa, pb);
-            iter(s + 1, pb, pa);
-        }
-        if (s < s_end) iter(s, pa, pb);
-    } else {
-        // T = 4 has no registers for two sets
-        for (int s = sb - T; s < s_end; ++s) {
-            iter(s, pa, pb);
-            pa = pb;
+        if constexpr (T <= 3) {
+            int s = sb - T;
+            for (; s + 1 < s_end; s += 2) {
+                iter(s, pa, pb);
+                iter(s + 1, pb, pa);
+            }
+            if (s < s_end) iter(s, pa, pb);
+        } else {
+            // T >= 4 has no registers for two sets
+            for (int s = sb - T; s < s_end; ++s) {
+                iter(s, pa, pb);
+                pa = pb;
+            }
         }
     }
     if (LAST && a.rrn) fused_rrn_reduce(racc, a.partials, a.counter, sc);
@@ -1363,16 +1378,18 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
             a.pitch = c->pitch;
             a.pitch64 = c->pitch;
             a.band = fused_band(T);
-            a.seg = c->inner_seg;
-            if (a.seg < 1) {
-                // automatic: one wave of 2 CTAs per SM with the longest segments
-                // (each segment recomputes 2T strips of pipeline warm-up)
-                const int bands = (c->nx + a.band - 1) / a.band;
-                const int per_col = (2 * c->sms) / bands > 1 ? (2 * c->sms) / bands : 1;
-                a.seg = (nstrips + per_col - 1) / per_col;
-                if (a.seg < 4 * T) a.seg = 4 * T;
+            a.nbands = (c->nx + a.band - 1) / a.band;
+            const long long work = (long long)a.nbands * nstrips;  // (band, strip) pairs
+            long long chunk = c->inner_seg;
+            if (chunk < 1) {
+                // automatic: equal shares for one wave of 2 CTAs per SM (each
+                // share recomputes 2T strips of pipeline warm-up, and 2T more
+                // where it goes on into the next band)
+                chunk = (work + 2 * c->sms - 1) / (2 * c->sms);
+                if (chunk < 4 * T) chunk = 4 * T;
             }
-            if ((nstrips + a.seg - 1) / a.seg > 65535) a.seg = (nstrips + 65534) / 65535;
+            if (chunk > nstrips) chunk = nstrips;
+            a.chunk = (int)chunk;
             a.sd_in = mx->sd[l & 1];
             a.sd_out = mx->sd[(l + 1) & 1];
             a.rt_in = rt[l & 1];
@@ -1392,13 +1409,14 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
             a.rs64 = c->r_store;
             a.partials = mx->fpartials;
             a.counter = mx->counter;
-            const dim3 fg((unsigned)((c->nx + a.band - 1) / a.band), (unsigned)((nstrips + a.seg - 1) / a.seg));
+            const dim3 fg((unsigned)((work + chunk - 1) / chunk));
             rc = launch_v(c, "mixed_pp_fused", [&] {
                 switch (T) {
                 case 1: launch_fused_pc<1>(fg, s, a, pc, last, c->sc); break;
                 case 2: launch_fused_pc<2>(fg, s, a, pc, last, c->sc); break;
                 case 3: launch_fused_pc<3>(fg, s, a, pc, last, c->sc); break;
-                default: launch_fused_pc<4>(fg, s, a, pc, last, c->sc); break;
+                case 4: launch_fused_pc<4>(fg, s, a, pc, last, c->sc); break;
+                default: launch_fused_pc<5>(fg, s, a, pc, last, c->sc); break;
                 }
             });
             if (rc) return rc;

@@ -104,12 +104,12 @@ def _fusion_runs(precond, settings):
 
 @pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
 def test_fused_inner_steps_are_bitwise_equal(precond):
-    """The temporally blocked inner steps (2-4 per pass, any segment height)
+    """The temporally blocked inner steps (2-5 per pass, any segment height)
     give the bits of one kernel per inner step; 600 x 150 cells make several
     column bands, a partial last strip and many row segments.  (The outer
     rrn sum stays in its own kernel here: fold_rrn off.)"""
     runs = _fusion_runs(precond, [(1, 32, False), (2, 32, False), (3, 4, False), (4, 4, False),
-                                  (4, 1, False), (2, 7, False), (4, 0, False)])
+                                  (4, 1, False), (2, 7, False), (4, 0, False), (5, 0, False), (5, 3, False)])
     its0, u0, fs0 = runs[(1, 32, False)]
     for key, (its, u, fs) in runs.items():
         assert its == its0, key
@@ -133,6 +133,6 @@ def test_folded_rrn_matches_to_round_off(precond):
 def test_inner_fusion_rejects_bad_settings():
     cfg = tl.parse_deck(decks.make_deck(x_cells=32, y_cells=32, end_step=1))
     with tl.Chunk(cfg) as ch:
-        for bad in [(0, 32, 1), (5, 32, 1), (2, -1, 1)]:
+        for bad in [(0, 32, 1), (6, 32, 1), (2, -1, 1)]:
             with pytest.raises(tl.TeaLeafError):
                 ch.set_inner_fusion(*bad)
