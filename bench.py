@@ -131,16 +131,21 @@ def bytes_per_cell(kernel, precond):
         # read r (FP64) + the preconditioner; write r, z, p, d
         return {"none": 24, "jac_diag": 28, "jac_block": 36}[precond]
     if kernel == "mixed_pp_ur":
-        # read u, p, w, r (FP64) + the FP32 preconditioner (Mi; or Ky, cp,
-        # bfp); write u, r (FP64) and rtemp, sd, utemp (FP32)
+        if FUSED_STEPS > 1:
+            # read u, p, w, r; write u, r (FP64): the first fused pass starts
+            # the inner steps from r itself
+            return 48
+        # + the FP32 preconditioner (Mi; or Ky, cp, bfp); write rtemp, sd,
+        # utemp (FP32)
         return {"none": 60, "jac_diag": 64, "jac_block": 72}[precond]
     if kernel == "mixed_pp_fused":
-        # the same arrays once per pass of several inner steps; the last pass
-        # of a solve writes z (FP64) instead of sd, rtemp and utemp (FP32):
+        # the same arrays once per pass of several inner steps; the first
+        # pass of a solve reads r (FP64) instead of sd, rtemp and utemp and
+        # the last one writes z (FP64) instead of sd, rtemp and utemp (FP32):
         # the mean over the INNER_STEPS / FUSED_STEPS passes of one solve
         passes = -(-INNER_STEPS // FUSED_STEPS)
         full = {"none": 32, "jac_diag": 36, "jac_block": 40}[precond]
-        return full - 4.0 / passes
+        return full - 8.0 / passes
     return BYTES_PER_CELL.get(kernel)
 
 

@@ -788,7 +788,11 @@ __device__ __forceinline__ float row_of(const float4 &v, int k) {
     return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
-template <int T, int PC, bool LAST>
+// LAST: the last pass of a solve (writes z in FP64).  FIRST: the first pass
+// of a solve, which starts the inner steps from r (FP64): rtemp = r, sd =
+// utemp = M^-1 r / theta (the start BodyPpUr<PC, true> writes), instead of
+// reading sd, rtemp and utemp
+template <int T, int PC, bool LAST, bool FIRST>
 __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs a, DevScalars *sc) {
     if (*(volatile const int *)&sc->done) return;
     constexpr int NT = fused_threads<T>();
@@ -807,6 +811,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
         be[t] = (float)a.betas[a.step0 + t - 1];
     }
     for (int k = tid; k < (R * NA + 2 * T) * SR; k += NT) smem4[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float theta_r = FIRST ? (float)(1.0 / sc->theta) : 0.f;
     double racc = 0.0;  // LAST with rrn: this thread's (r - r_store).z
     // the CTA's share of the band-major sequence of (band, strip) pairs: a
     // share that reaches the end of a band goes on at the top of the next
@@ -831,6 +836,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
         struct Pipe {
             float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
             float ldS[4], ldR[4], ldU[4], ldC[NA][4];
+            double ldR64[FIRST ? 4 : 1];  // FIRST: r (FP64) in place of sd, rtemp, utemp
         };
         Pipe pa, pb;
 #pragma unroll
@@ -847,9 +853,13 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                 const int row = 4 * s + k;
                 const bool v = incol && s >= 0 && row < a.ny;
                 const int i = cbase + (row + a.h) * a.pitch;
-                o.ldS[k] = v ? a.sd_in[i] : 0.f;
-                o.ldR[k] = v ? a.rt_in[i] : 0.f;
-                o.ldU[k] = v ? a.utemp[i] : 0.f;
+                if constexpr (FIRST) {
+                    o.ldR64[k] = v ? a.r64[(int64_t)cbase + (int64_t)(row + a.h) * a.pitch64] : 0.0;
+                } else {
+                    o.ldS[k] = v ? a.sd_in[i] : 0.f;
+                    o.ldR[k] = v ? a.rt_in[i] : 0.f;
+                    o.ldU[k] = v ? a.utemp[i] : 0.f;
+                }
                 o.ldC[0][k] = v ? __ldg(&a.kx[i]) : 0.f;
                 o.ldC[1][k] = v ? __ldg(&a.ky[i]) : 0.f;
                 if (PC == TL_PREC_JAC_BLOCK) {
@@ -874,13 +884,20 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                                      : pf_arr == 4 ? a.ky
                                      : pf_arr == 5 ? (PC == TL_PREC_JAC_BLOCK ? a.cp : a.mi)
                                                    : a.bfp;
-        const bool pf_on = pf_arr < NA + 3 && wc0 <= wc1;
+        // (the first pass reads r (FP64) in place of sd, rtemp and utemp)
+        const bool pf_on = pf_arr < NA + 3 && wc0 <= wc1 && !(FIRST && (pf_arr == 1 || pf_arr == 2));
         auto prefetch = [&](int s2) {
             const int row = 4 * s2 + pf_k;
             if (pf_on && s2 >= 0 && row < a.ny) {
-                const float *p = pf_base + (row + a.h) * a.pitch + a.h;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc0));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc1));
+                if (FIRST && pf_arr == 0) {
+                    const double *p = a.r64 + (int64_t)(row + a.h) * a.pitch64 + a.h;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc0));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc1));
+                } else {
+                    const float *p = pf_base + (row + a.h) * a.pitch + a.h;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc0));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + wc1));
+                }
             }
         };
         load(sb - T, pa);
@@ -892,9 +909,46 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
         // one strip iteration: level 0 takes strip s from `in`, levels 1..T
         // advance, and what the next iteration needs goes to `out`
         auto iter = [&](const int s, const Pipe &in, Pipe &out) {
+            // level 0's strip s: sd, rtemp, utemp
+            float s0[4], r0[4], u0[4];
+            if constexpr (FIRST) {
+                // the start of the inner steps from r on the strip's mm rows:
+                // rtemp = r, z = M^-1 rtemp, sd = utemp = z / theta (BodyPpUr's
+                // operations, row for row)
+                const int mm = (incol && s >= 0) ? max(0, min(4, a.ny - 4 * s)) : 0;
+                float zf[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    r0[k] = (float)in.ldR64[k];
+                    zf[k] = 0.f;
+                }
+                if constexpr (PC == TL_PREC_JAC_BLOCK) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < mm)
+                            zf[k] = k == 0 ? r0[0] * in.ldC[3][0]
+                                           : fmaf(in.ldC[1][k], zf[k > 0 ? k - 1 : 0], r0[k]) * in.ldC[3][k];
+#pragma unroll
+                    for (int k = 2; k >= 0; --k)
+                        if (k < mm - 1) zf[k] = fmaf(-in.ldC[2][k], zf[k + 1], zf[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (k < mm) zf[k] = PC == TL_PREC_JAC_DIAG ? r0[k] * in.ldC[NA - 1][k] : r0[k];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) s0[k] = u0[k] = k < mm ? zf[k] * theta_r : 0.f;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    s0[k] = in.ldS[k];
+                    r0[k] = in.ldR[k];
+                    u0[k] = in.ldU[k];
+                }
+            }
             {
                 float4 *cf = cfb + slot * NA * SR + tid;
-                xsb[(s & 1) * SR + tid] = make_float4(in.ldS[0], in.ldS[1], in.ldS[2], in.ldS[3]);
+                xsb[(s & 1) * SR + tid] = make_float4(s0[0], s0[1], s0[2], s0[3]);
 #pragma unroll
                 for (int q = 0; q < NA; ++q)
                     cf[q * SR] = make_float4(in.ldC[q][0], in.ldC[q][1], in.ldC[q][2], in.ldC[q][3]);
@@ -910,9 +964,9 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                 float cS[4], cR[4], cU[4];  // level t-1's output of this iteration
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    cS[k] = in.ldS[k];
-                    cR[k] = in.ldR[k];
-                    cU[k] = in.ldU[k];
+                    cS[k] = s0[k];
+                    cR[k] = r0[k];
+                    cU[k] = u0[k];
                 }
 #pragma unroll
                 for (int t = 1; t <= T; ++t) {
@@ -1130,8 +1184,10 @@ struct BodyUpdateU {  // u += d (FP64)
 // u += alpha p, r -= alpha w (FP64, as BodyCgUr of tl_kernels.cu), then
 // rtemp = r, z = M^-1 r and sd = utemp = z / theta in FP32 (as k_pp_init):
 // z only seeds the FP32 polynomial preconditioner, so M^-1 uses the FP32
-// operator copies (the block solve of k_pp_step, 1/diag in bfp's first row)
-template <int PC>
+// operator copies (the block solve of k_pp_step, 1/diag in bfp's first row).
+// START false: the u / r update alone (the first fused inner pass then
+// starts the inner steps from r itself)
+template <int PC, bool START>
 struct BodyPpUr {
     const double *p, *w;
     double *u, *r;
@@ -1158,7 +1214,8 @@ struct BodyPpUr {
                 pv[k] = p[i];
                 wv[k] = w[i];
                 rv[k] = r[i];
-                if (PC == TL_PREC_JAC_BLOCK) {
+                if (!START) {
+                } else if (PC == TL_PREC_JAC_BLOCK) {
                     kyv[k] = ky[j];
                     cpv[k] = cp[j];
                     bfv[k] = bfp[j];
@@ -1175,6 +1232,7 @@ struct BodyPpUr {
                 r[i] = rv[k];
                 rf[k] = (float)rv[k];
             }
+        if (!START) return;
         if (PC == TL_PREC_JAC_BLOCK) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
@@ -1316,29 +1374,32 @@ int mixed_ppcg_prepare(Chunk *c) {
     });
 }
 
-template <int T, int PC, bool LAST>
+template <int T, int PC, bool LAST, bool FIRST>
 void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, DevScalars *sc) {
     constexpr size_t bytes = fused_smem<T, PC>();
     static bool configured = false;  // the attribute belongs to the kernel: set once
     if (!configured) {
-        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST, FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST, FIRST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         configured = true;
     }
-    k_pp_fused<T, PC, LAST><<<grid, fused_threads<T>(), bytes, s>>>(a, sc);
+    k_pp_fused<T, PC, LAST, FIRST><<<grid, fused_threads<T>(), bytes, s>>>(a, sc);
 }
 
 template <int T, int PC>
-void launch_fused(dim3 grid, cudaStream_t s, const PpFusedArgs &a, bool last, DevScalars *sc) {
-    if (last) launch_fused1<T, PC, true>(grid, s, a, sc);
-    else launch_fused1<T, PC, false>(grid, s, a, sc);
+void launch_fused(dim3 grid, cudaStream_t s, const PpFusedArgs &a, bool last, bool first, DevScalars *sc) {
+    if (last && first) launch_fused1<T, PC, true, true>(grid, s, a, sc);
+    else if (last) launch_fused1<T, PC, true, false>(grid, s, a, sc);
+    else if (first) launch_fused1<T, PC, false, true>(grid, s, a, sc);
+    else launch_fused1<T, PC, false, false>(grid, s, a, sc);
 }
 
 template <int T>
-void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bool last, DevScalars *sc) {
-    if (pc == TL_PREC_JAC_BLOCK) launch_fused<T, TL_PREC_JAC_BLOCK>(grid, s, a, last, sc);
-    else if (pc == TL_PREC_JAC_DIAG) launch_fused<T, TL_PREC_JAC_DIAG>(grid, s, a, last, sc);
-    else launch_fused<T, TL_PREC_NONE>(grid, s, a, last, sc);
+void launch_fused_pc(dim3 grid, cudaStream_t s, const PpFusedArgs &a, int pc, bool last, bool first,
+                     DevScalars *sc) {
+    if (pc == TL_PREC_JAC_BLOCK) launch_fused<T, TL_PREC_JAC_BLOCK>(grid, s, a, last, first, sc);
+    else if (pc == TL_PREC_JAC_DIAG) launch_fused<T, TL_PREC_JAC_DIAG>(grid, s, a, last, first, sc);
+    else launch_fused<T, TL_PREC_NONE>(grid, s, a, last, first, sc);
 }
 
 // the inner steps of tea_leaf_ppcg.f90:174-230 in FP32; z (FP64) at the end.
@@ -1350,7 +1411,16 @@ namespace {
 // the inner steps proper, from sd[0], rtemp, utemp to z (FP64)
 // rrn: the last fused pass also sums (r - r_store).z and updates the PPCG
 // scalars (*did_rrn reports whether it did: only fused passes can)
-int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
+// FP32 inner steps per fused pass (1: one kernel per step).  The fused
+// kernel addresses FP32 fields with 32-bit offsets; fields of 2^31 elements
+// or more take the one-kernel-per-step path (64-bit)
+int fused_steps(const Chunk *c) {
+    const bool fits32 = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows < ((size_t)1 << 31);
+    return !fits32 ? 1 : c->inner_fuse < 1 ? 1 : (c->inner_fuse > kFusedMax ? kFusedMax : c->inner_fuse);
+}
+
+// first: the first fused pass starts the inner steps from r (FP64) itself
+int inner_steps(Chunk *c, bool rrn, bool *did_rrn, bool first) {
     Mixed *mx = mixed_of(c);
     *did_rrn = false;
     const int inner = c->cfg.ppcg_inner_steps;
@@ -1359,10 +1429,7 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
     cudaStream_t s = c->stream;
     const int pc = c->cfg.precond;
     int rc;
-    // the fused kernel addresses FP32 fields with 32-bit offsets; fields of
-    // 2^31 elements or more take the one-kernel-per-step path (64-bit)
-    const bool fits32 = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows < ((size_t)1 << 31);
-    const int fuse = !fits32 ? 1 : c->inner_fuse < 1 ? 1 : (c->inner_fuse > kFusedMax ? kFusedMax : c->inner_fuse);
+    const int fuse = fused_steps(c);
     if (fuse > 1) {
         float *rt[2] = {mx->rtemp, mx->rtemp2};
         const int passes = (inner + fuse - 1) / fuse;
@@ -1403,6 +1470,7 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
             a.alphas = c->ch_alphas;
             a.betas = c->ch_betas;
             a.step0 = done + 1;
+            const bool fst = first && l == 0;
             a.z64 = c->z;
             a.rrn = (rrn && last) ? 1 : 0;
             a.r64 = c->r;
@@ -1412,11 +1480,11 @@ int inner_steps(Chunk *c, bool rrn, bool *did_rrn) {
             const dim3 fg((unsigned)((work + chunk - 1) / chunk));
             rc = launch_v(c, "mixed_pp_fused", [&] {
                 switch (T) {
-                case 1: launch_fused_pc<1>(fg, s, a, pc, last, c->sc); break;
-                case 2: launch_fused_pc<2>(fg, s, a, pc, last, c->sc); break;
-                case 3: launch_fused_pc<3>(fg, s, a, pc, last, c->sc); break;
-                case 4: launch_fused_pc<4>(fg, s, a, pc, last, c->sc); break;
-                default: launch_fused_pc<5>(fg, s, a, pc, last, c->sc); break;
+                case 1: launch_fused_pc<1>(fg, s, a, pc, last, fst, c->sc); break;
+                case 2: launch_fused_pc<2>(fg, s, a, pc, last, fst, c->sc); break;
+                case 3: launch_fused_pc<3>(fg, s, a, pc, last, fst, c->sc); break;
+                case 4: launch_fused_pc<4>(fg, s, a, pc, last, fst, c->sc); break;
+                default: launch_fused_pc<5>(fg, s, a, pc, last, fst, c->sc); break;
                 }
             });
             if (rc) return rc;
@@ -1478,22 +1546,28 @@ int mixed_ppcg_inner(Chunk *c) {
          })))
         return rc;
     bool did_rrn;
-    return inner_steps(c, false, &did_rrn);
+    return inner_steps(c, false, &did_rrn, false);
 }
 
 int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn) {
     if (!inner_ready(c)) return TL_ERR_STATE;
     Mixed *mx = mixed_of(c);
     int rc;
-#define TL_PP_UR(PC)                                                                                       \
-    BodyPpUr<PC>{c->p, c->w, c->u, c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->sd[0], mx->rtemp, mx->utemp, \
-                 c->pitch, c->pitch, 0.0, 0.f}
-    if (c->cfg.precond == TL_PREC_JAC_BLOCK) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_BLOCK), kInNone, true);
-    else if (c->cfg.precond == TL_PREC_JAC_DIAG) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_DIAG), kInNone, true);
-    else rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_NONE), kInNone, true);
+    // with fused passes the first pass starts the inner steps from r, and
+    // this pass only updates u and r
+    const bool start = fused_steps(c) == 1;
+#define TL_PP_UR(PC, S)                                                                                       \
+    BodyPpUr<PC, S>{c->p, c->w, c->u, c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->sd[0], mx->rtemp, mx->utemp, \
+                    c->pitch, c->pitch, 0.0, 0.f}
+    if (!start) rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_NONE, false), kInNone, true);
+    else if (c->cfg.precond == TL_PREC_JAC_BLOCK)
+        rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_BLOCK, true), kInNone, true);
+    else if (c->cfg.precond == TL_PREC_JAC_DIAG)
+        rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_JAC_DIAG, true), kInNone, true);
+    else rc = run32(c, "mixed_pp_ur", TL_PP_UR(TL_PREC_NONE, true), kInNone, true);
 #undef TL_PP_UR
     if (rc) return rc;
-    return inner_steps(c, c->inner_fold_rrn, did_rrn);
+    return inner_steps(c, c->inner_fold_rrn, did_rrn, !start);
 }
 
 int mixed_ppcg_presteps(Chunk *c, int *done_out) {
