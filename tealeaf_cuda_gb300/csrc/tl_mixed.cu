@@ -727,7 +727,8 @@ struct PpFusedArgs {
 
 // CTA + grid sum of the fused pass's rrn (deterministic: warps, then CTAs,
 // in index order); the last CTA updates the PPCG scalars as the FP64
-// path's ppcg_rrn epilogue does: rrn, beta = rrn / rro, error = rro = rrn.
+// path's ppcg_rrn epilogue does: rrn, beta = rrn / rro, error = rro = rrn,
+// one more outer iteration.
 // Every thread of the CTA calls it.
 __device__ void fused_rrn_reduce(double acc, double *partials, unsigned int *counter, DevScalars *sc) {
     __shared__ double sh[kFusedThreadsMax / 32];
@@ -763,6 +764,7 @@ __device__ void fused_rrn_reduce(double acc, double *partials, unsigned int *cou
         sc->beta = tot / sc->rro;
         sc->error = tot;
         sc->rro = tot;
+        sc->ppcg_iters += 1;
         __threadfence();
         *counter = 0u;
     }
@@ -845,7 +847,8 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
 #pragma unroll
             for (int k = 0; k < 4; ++k) pa.sdP[l][k] = pa.rtP[l][k] = pa.utP[l][k] = 0.f;
         }
-        // level 0 loads, one strip ahead (32-bit offsets: a field has < 2^31 elements)
+        // level 0 loads, one strip ahead (32-bit offsets, FP64 fields too: a
+        // field has < 2^31 elements)
         const int cbase = col + a.h;
         auto load = [&](int s, Pipe &o) {
 #pragma unroll
@@ -854,7 +857,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                 const bool v = incol && s >= 0 && row < a.ny;
                 const int i = cbase + (row + a.h) * a.pitch;
                 if constexpr (FIRST) {
-                    o.ldR64[k] = v ? a.r64[(int64_t)cbase + (int64_t)(row + a.h) * a.pitch64] : 0.0;
+                    o.ldR64[k] = v ? a.r64[cbase + (row + a.h) * a.pitch64] : 0.0;
                 } else {
                     o.ldS[k] = v ? a.sd_in[i] : 0.f;
                     o.ldR[k] = v ? a.rt_in[i] : 0.f;
@@ -1051,7 +1054,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                             if (k < m) {
                                 const int row = 4 * q + k;
                                 if (LAST) {
-                                    const int64_t i64 = (int64_t)cbase + (int64_t)(row + a.h) * a.pitch64;
+                                    const int i64 = cbase + (row + a.h) * a.pitch64;
                                     const double zv = (double)oU[k];
                                     a.z64[i64] = zv;
                                     if (a.rrn) racc = fma(a.r64[i64] - a.rs64[i64], zv, racc);
