@@ -80,6 +80,7 @@ BYTES_PER_CELL = {
     "field_summary": 32,
     "finalise": 24,
     "ppcg_p": 24,        # read z, p; write p
+    "ppcg_up": 40,       # read p, u, z; write u, p (mixed PPCG with fused inner passes)
     "ppcg_update_r": 48,  # read sd, Kx, Ky, diag, rtemp; write rtemp
     "cheby_calc_u": 24,  # read u, p; write u
     "copy": 16,          # read src; write dst
@@ -132,9 +133,9 @@ def bytes_per_cell(kernel, precond):
         return {"none": 24, "jac_diag": 28, "jac_block": 36}[precond]
     if kernel == "mixed_pp_ur":
         if FUSED_STEPS > 1:
-            # read u, p, w, r; write u, r (FP64): the first fused pass starts
-            # the inner steps from r itself
-            return 48
+            # read w, r; write r (FP64): the first fused pass starts the inner
+            # steps from r itself and u += alpha p runs in ppcg_up
+            return 24
         # + the FP32 preconditioner (Mi; or Ky, cp, bfp); write rtemp, sd,
         # utemp (FP32)
         return {"none": 60, "jac_diag": 64, "jac_block": 72}[precond]

@@ -192,6 +192,7 @@ int launch_copy(Chunk *c, double *dst, const double *src, bool fast);
 int launch_ppcg_rrn(Chunk *c, int epi, bool fast);
 int launch_ppcg_zr(Chunk *c, int epi, bool fast);
 int launch_ppcg_w_store_zr(Chunk *c, bool fast, bool five);  // cg_w + ppcg_store_zr, one pass
+int launch_ppcg_up(Chunk *c, int epi, bool fast);  // u += alpha p, p = z + beta p (mixed, fused passes)
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast);
 int launch_jacobi(Chunk *c, int epi, bool fast);
 int launch_finalise(Chunk *c);
@@ -230,6 +231,9 @@ int mixed_ppcg_inner(Chunk *c);    // PPCG inner steps in FP32, z in FP64
 // the outer u/r update fused with the inner start, then the steps; *did_rrn
 // tells whether the last pass also summed (r - r_store).z (kEpiPpcgRrn)
 int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn);
+// whether mixed PPCG runs its inner steps as fused passes: its outer pass
+// then updates r alone, and u += alpha p moves into the p pass (launch_ppcg_up)
+bool mixed_fused(const Chunk *c);
 void drop_graphs(Chunk *c);        // after a change that captured graphs depend on
 constexpr int kFusedMax = 5;           // most FP32 PPCG inner steps fused into one pass
 constexpr int kInnerFuseDefault = 5;

@@ -434,6 +434,39 @@ struct BodyAxpyP {  // p = src + beta p  (tea_leaf_cg.cuknl:141-161, tea_leaf_pp
     }
 };
 
+// mixed PPCG with fused inner passes: u += alpha p (the u half of the outer
+// update, tea_leaf_cg.cuknl:72-137), then p = z + beta p
+// (tea_leaf_ppcg.cuknl:301-313), in one pass over the old p
+struct BodyPpcgUP {
+    double *p, *u;
+    const double *z;
+    const double *alpha_p, *beta_p;
+    int pitch;
+    double alpha, beta;
+    __device__ void setup() {
+        alpha = *alpha_p;
+        beta = *beta_p;
+    }
+    __device__ void operator()(int64_t base, int m, double (&acc)[1]) const {
+        double pv[4], uv[4], zv[4];  // loads first: see BodyCgUr
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = base + (int64_t)k * pitch;
+                pv[k] = p[i];
+                uv[k] = u[i];
+                zv[k] = z[i];
+            }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < m) {
+                const int64_t i = base + (int64_t)k * pitch;
+                u[i] = fma(alpha, pv[k], uv[k]);
+                p[i] = fma(beta, pv[k], zv[k]);
+            }
+    }
+};
+
 template <int PC>
 struct BodyChebyInitP {  // tea_leaf_cheby.cuknl:5-68
     const double *dg;  // diag(A), stored by the diag kernel
@@ -1102,6 +1135,11 @@ int launch_ppcg_w_store_zr(Chunk *c, bool fast, bool five) {
     }
     BodyCgWStoreZr<false> b{c->diag, c->p, c->kx, c->ky, c->r, c->z, c->w, c->r_store, c->pitch};
     return run<2>(c, "ppcg_w_zr", b, kEpiPwZr, fast);
+}
+
+int launch_ppcg_up(Chunk *c, int epi, bool fast) {
+    BodyPpcgUP b{c->p, c->u, c->z, &c->sc->alpha, &c->sc->beta, c->pitch, 0.0, 0.0};
+    return run<1>(c, "ppcg_up", b, epi, fast);
 }
 
 int launch_ppcg_p(Chunk *c, double beta, int epi, bool fast) {

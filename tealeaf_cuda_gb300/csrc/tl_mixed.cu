@@ -1188,8 +1188,9 @@ struct BodyUpdateU {  // u += d (FP64)
 // rtemp = r, z = M^-1 r and sd = utemp = z / theta in FP32 (as k_pp_init):
 // z only seeds the FP32 polynomial preconditioner, so M^-1 uses the FP32
 // operator copies (the block solve of k_pp_step, 1/diag in bfp's first row).
-// START false: the u / r update alone (the first fused inner pass then
-// starts the inner steps from r itself)
+// START false: the r update alone (the first fused inner pass then starts
+// the inner steps from r itself, and u += alpha p runs in the p pass,
+// BodyPpcgUP)
 template <int PC, bool START>
 struct BodyPpUr {
     const double *p, *w;
@@ -1213,8 +1214,10 @@ struct BodyPpUr {
             if (k < m) {
                 const int64_t i = b64 + (int64_t)k * pitch64;
                 const int64_t j = b32 + (int64_t)k * pitch32;
-                uv[k] = u[i];
-                pv[k] = p[i];
+                if (START) {
+                    uv[k] = u[i];
+                    pv[k] = p[i];
+                }
                 wv[k] = w[i];
                 rv[k] = r[i];
                 if (!START) {
@@ -1230,7 +1233,7 @@ struct BodyPpUr {
         for (int k = 0; k < 4; ++k)
             if (k < m) {
                 const int64_t i = b64 + (int64_t)k * pitch64;
-                u[i] = fma(alpha, pv[k], uv[k]);
+                if (START) u[i] = fma(alpha, pv[k], uv[k]);
                 rv[k] = fma(-alpha, wv[k], rv[k]);
                 r[i] = rv[k];
                 rf[k] = (float)rv[k];
@@ -1552,12 +1555,14 @@ int mixed_ppcg_inner(Chunk *c) {
     return inner_steps(c, false, &did_rrn, false);
 }
 
+bool mixed_fused(const Chunk *c) { return fused_steps(c) > 1; }
+
 int mixed_ppcg_ur_inner(Chunk *c, bool *did_rrn) {
     if (!inner_ready(c)) return TL_ERR_STATE;
     Mixed *mx = mixed_of(c);
     int rc;
     // with fused passes the first pass starts the inner steps from r, and
-    // this pass only updates u and r
+    // this pass only updates r (u += alpha p runs in the p pass)
     const bool start = fused_steps(c) == 1;
 #define TL_PP_UR(PC, S)                                                                                       \
     BodyPpUr<PC, S>{c->p, c->w, c->u, c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->sd[0], mx->rtemp, mx->utemp, \

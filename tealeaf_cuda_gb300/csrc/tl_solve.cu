@@ -83,7 +83,9 @@ int body_ppcg(Chunk *c) {
         if ((rc = ppcg_inner_steps(c, true))) return rc;
     }
     if (!did_rrn && (rc = launch_ppcg_rrn(c, kEpiPpcgRrn, true))) return rc;
-    if ((rc = launch_ppcg_p(c, 0.0, kEpiFinishNoSwitch, true))) return rc;
+    if (mixed && mixed_fused(c)) rc = launch_ppcg_up(c, kEpiFinishNoSwitch, true);
+    else rc = launch_ppcg_p(c, 0.0, kEpiFinishNoSwitch, true);
+    if (rc) return rc;
     return halo(c, TL_FIELD_P, 1);
 }
 
