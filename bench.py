@@ -98,10 +98,11 @@ BYTES_PER_CELL = {
 
 
 # DRAM bytes per cell measured by ncu (dram__bytes_read.sum + write.sum of one
-# launch / cells), for the kernels that can dominate the default workload;
+# launch / cells), for the kernels that can dominate the default workload
+# (mixed_pp_fused measured at the workload's own 8192^2, cg_w at 4096^2);
 # scaled to a launch by the cells it processes
 TRAFFIC_PER_CELL = {
-    "mixed_pp_fused": 37.5,   # k_pp_fused<3, jac_block> at 4096^2: 514.8 + 115.3 MB
+    "mixed_pp_fused": 42.98,  # k_pp_fused<5, jac_block> first + last pass at 8192^2: mean 2884.2 MB a launch
     "cg_w": 39.6,             # BodyCgW at 4096^2: 545.5 + 119.4 MB
 }
 

@@ -183,8 +183,9 @@ int tl_set_profiling(tl_chunk_t *ch, int on);
 int tl_profile_reset(tl_chunk_t *ch);
 /* mixed-precision PPCG: run `steps` (1..5) FP32 inner steps per pass over
  * HBM (temporal blocking; 1 = one kernel per inner step), each CTA taking
- * `seg_strips` 4-row strips of a column band (0: chosen from the grid size,
- * one wave of CTAs).  The inner steps give the same bits for every setting.
+ * `seg_strips` 4-row strips of the band-major sequence of (column band,
+ * strip) pairs (0: equal shares for one wave of CTAs).  The inner steps
+ * give the same bits for every setting.
  * fold_rrn != 0 lets the last fused pass also sum the outer (r - r_store).z,
  * saving a pass over r, r_store and z; that sum then runs in the fused
  * grid's order, so solves with different settings agree to round-off rather
