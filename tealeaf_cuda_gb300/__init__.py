@@ -247,7 +247,7 @@ class Chunk:
         _check(load().tl_set_dt(self._h, dt), "tl_set_dt")
 
     def set_inner_fusion(self, steps, seg_strips=0, fold_rrn=False):
-        """FP32 PPCG inner steps per HBM pass (1..5), strips per CTA segment
+        """FP32 PPCG inner steps per HBM pass (1..5), strips per CTA share
         (0: automatic), and whether the last pass also sums PPCG's rrn"""
         _check(load().tl_set_inner_fusion(self._h, steps, seg_strips, 1 if fold_rrn else 0),
                "tl_set_inner_fusion")

@@ -130,7 +130,7 @@ struct Chunk {
     // mixed precision state (allocated on first use)
     void *mixed;
     int inner_fuse;              // FP32 PPCG inner steps per HBM pass (1: one kernel per step)
-    int inner_seg;               // 4-row strips per CTA segment of the fused inner kernel (0: automatic)
+    int inner_seg;               // 4-row strips per CTA share of the fused inner kernel (0: automatic)
     bool inner_fold_rrn;         // the last fused inner pass also sums PPCG's rrn
     int sms;                     // multiprocessors of the device
     // learned warm start model and buffers (tl_warm.cu)

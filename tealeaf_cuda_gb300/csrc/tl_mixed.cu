@@ -664,11 +664,13 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 //
 // T inner steps per pass over HBM (the matrix-powers idea of the
 // reference's halo_depth > 1 PPCG, tea_leaf_ppcg.f90:199-221, done inside one
-// chunk).  A CTA owns a band of fused_threads<T>() columns (one column per
-// thread, T columns of halo on each side, recomputed) and a segment of
-// `seg` 4-row strips, and streams down the strips as a pipeline: at
+// chunk).  A CTA spans fused_threads<T>() columns (one column per thread:
+// a band of owned columns and T columns of halo on each side, recomputed)
+// and takes an equal share of the band-major sequence of (band, 4-row
+// strip) pairs.  It streams down the strips of its share as a pipeline: at
 // iteration s, level 0 takes strip s (sd, rtemp, utemp and the strip's
-// coefficients, loaded from HBM during iteration s-1) and level t = 1..T
+// coefficients, loaded from HBM during iteration s-1; the strip after that
+// is prefetched into L2) and level t = 1..T
 // applies inner step t to strip s - t, from level t-1's strips s-t-1 (last
 // row), s-t and s-t+1 (first row).  Vertical neighbours stay in the
 // thread's registers; horizontal ones go through shared memory (a buffer
@@ -678,7 +680,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_pp_step(
 // memory keeps a column's strip as one float4 (its 4 rows) per array, so a
 // level reads its coefficients, its west and east neighbours' sd and the
 // east neighbour's Kx with one 16-byte load each.  Level T
-// stores its strip when it lies in the CTA's band and segment.  sd and rtemp
+// stores its strip when it lies in the CTA's band and share.  sd and rtemp
 // are read in halos that other CTAs own, so they ping-pong between launches;
 // utemp is read and written only at owned cells (its halo values are never
 // stored) and is updated in place.  Every value is computed with the
@@ -1290,7 +1292,7 @@ int mixed_alloc(Chunk *c) {
     TL_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * (size_t)mx->vtiles + 256, c->stream));
     mx->counter = (unsigned int *)p;
     mx->partials = (double *)((char *)p + 256);
-    // the most CTAs a fused pass can have: the narrowest band, one strip per segment
+    // the most CTAs a fused pass can have: the narrowest band, one strip per share
     const size_t fcta = (size_t)((c->nx + kFusedBandMin - 1) / kFusedBandMin) * (size_t)((c->ny + 3) / 4);
     e = cudaMalloc(&p, sizeof(double) * fcta);
     if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");

@@ -105,9 +105,9 @@ def _fusion_runs(precond, settings):
 
 @pytest.mark.parametrize("precond", ["none", "jac_diag", "jac_block"])
 def test_fused_inner_steps_are_bitwise_equal(precond):
-    """The temporally blocked inner steps (2-5 per pass, any segment height)
+    """The temporally blocked inner steps (2-5 per pass, any share size)
     give the bits of one kernel per inner step; 600 x 150 cells make several
-    column bands, a partial last strip and many row segments.  (The outer
+    column bands, a partial last strip and many shares.  (The outer
     rrn sum stays in its own kernel here: fold_rrn off.)"""
     runs = _fusion_runs(precond, [(1, 32, False), (2, 32, False), (3, 4, False), (4, 4, False),
                                   (4, 1, False), (2, 7, False), (4, 0, False), (5, 0, False), (5, 3, False)])
