@@ -27,6 +27,23 @@ def test_bench_decks_parse():
     assert bench.bytes_per_cell("cg_w", "jac_diag") == 32
 
 
+def test_bench_fused_pass_bytes():
+    """The fused inner passes' byte figure is the mean over one solve's
+    passes: a full pass reads sd, rtemp, utemp (12 B) and the coefficients
+    and writes sd, rtemp, utemp (12 B); the first reads r (FP64, 8 B)
+    instead of sd, rtemp, utemp and the last writes z (FP64, 8 B) instead of
+    them."""
+    assert bench.INNER_STEPS == 10 and bench.FUSED_STEPS == 5
+    coef = {"none": 8, "jac_diag": 12, "jac_block": 16}
+    for pc, c in coef.items():
+        first = 8 + c + 12
+        last = 12 + c + 8
+        assert bench.bytes_per_cell("mixed_pp_fused", pc) == (first + last) / 2, pc
+    # the outer pass then updates r alone, and u moves into the p pass
+    assert bench.bytes_per_cell("mixed_pp_ur", "jac_block") == 24
+    assert bench.bytes_per_cell("ppcg_up", "jac_block") == 40
+
+
 def test_reference_arm_prints_contract_line():
     env = dict(os.environ, OMP_NUM_THREADS="2")
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "64",
