@@ -96,3 +96,23 @@ def test_oracle_chebyshev_coefficients_follow_the_closed_form(eigmin, eigmax):
     if sigma > 1.01:
         limit = sigma - np.sqrt(sigma * sigma - 1.0)
         assert al[-1] == pytest.approx(limit * limit, rel=1e-12)
+
+
+@pytest.mark.parametrize("method", [dict(tl_use_cg=True, tl_preconditioner_type="jac_diag"),
+                                    dict(tl_use_cg=False, tl_use_ppcg=True, tl_preconditioner_type="jac_block",
+                                         tl_ppcg_inner_steps=10, tl_ch_cg_presteps=10, tl_ch_cg_epslim=1.0e10)])
+def test_oracle_is_independent_of_its_thread_count(method):
+    """The oracle's sums run per row in x order, then over rows in y order,
+    so a solve gives the same bits on 1 and on 4 threads (the grid is above
+    the size where its loops go parallel)."""
+    from tests import decks
+    from tests.oracle_run import run_deck
+    deck = decks.make_deck(n=300, end_step=2, summary_frequency=1, **method)
+    one, _ = run_deck(deck, threads=1)
+    four, _ = run_deck(deck, threads=4)
+    keys = ("iterations", "ppcg_inner", "switch_n", "error_ratio", "vol", "mass", "ie", "temp")
+    assert len(one) == len(four) == 3  # the step-0 summary and two timesteps
+    assert all(r["iterations"] > 10 for r in one[1:])
+    for a, b in zip(one, four):
+        for k in keys:
+            assert a.get(k) == b.get(k), k
