@@ -109,3 +109,35 @@ def test_calls_without_a_chunk_fail_with_status():
         lib.tea_leaf_cg_calc_w_kernel_cuda_(C.byref(pw))
         assert "initialise_cuda_" in tl.last_error()
         assert pw.value == -1.0
+
+
+def test_integration_c_example_compiles_and_links(tmp_path):
+    """The C usage of INTEGRATION.md (deck text -> config -> chunk -> start ->
+    timestep -> field summary) compiles as C11 against the public header and
+    links against the library (it is not run: that needs a GPU)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "example.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "tealeaf_capi.h"
+int run(const char *deck_text) {
+    tl_config_t cfg; char err[256];
+    if (tl_parse_deck(deck_text, &cfg, err, sizeof err) != TL_OK) { fprintf(stderr, "%s\n", err); return 1; }
+    tl_chunk_t *ch; if (tl_chunk_create(&cfg, &ch) != TL_OK) return 1;
+    double vol, mass, ie, temp; tl_start(ch, &vol, &mass, &ie, &temp);
+    tl_solve_info_t info; int rc = tl_timestep(ch, &info);
+    tl_field_summary(ch, &vol, &mass, &ie, &temp);
+    tl_chunk_destroy(ch);
+    return rc < 0;
+}
+int main(void) { return run("*tea\nstate 1 density=100.0 energy=0.0001\nx_cells=8\ny_cells=8\n*endtea\n"); }
+''')
+    build = os.path.join(ROOT, "tealeaf_cuda_gb300", "_build")
+    out = tmp_path / "example"
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-L", build, "-ltealeaf_gb300", "-o", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
