@@ -279,8 +279,9 @@ def oracle_sample(n, iters, steps, threads=None):
 
 
 def run_reference(args):
-    rank, ws, local = dist_init()
-    if rank != 0:
+    # the CPU oracle runs on rank 0 alone and needs no collective: the rank
+    # comes from the launcher's environment, with no process group
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     n = args.n
     per, threads = oracle_sample(n, args.ref_iters, args.warmup + args.steps)

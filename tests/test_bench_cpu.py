@@ -58,3 +58,56 @@ def test_reference_arm_prints_contract_line():
     assert d["impl"] == "reference" and d["steps"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["unit"] == d["unit"]
+
+
+_DIST_PROBE = r"""
+import json, os, sys
+sys.path.insert(0, os.environ["TL_ROOT"])
+import bench
+rank, ws, local = bench.dist_init()
+bench.barrier(ws)
+mx = bench.allreduce_max(rank + 1.5, ws, local)
+sm = bench.allreduce_sum(rank + 1.0, ws, local)
+bench.barrier(ws)
+print(json.dumps({"rank": rank, "ws": ws, "max": mx, "sum": sm}))
+import torch.distributed as dist
+dist.destroy_process_group()
+"""
+
+
+def _free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_bench_rank_helpers_over_gloo_world_size_2():
+    """bench.py's rank set-up, barrier and max / sum over ranks (the timing
+    max and the whole-job sum of its N>1 replicas) on two gloo ranks."""
+    port = str(_free_port())
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, TL_ROOT=ROOT, TL_BENCH_GLOO="1", RANK=str(rank), LOCAL_RANK=str(rank),
+                   WORLD_SIZE="2", MASTER_ADDR="127.0.0.1", MASTER_PORT=port)
+        procs.append(subprocess.Popen([sys.executable, "-c", _DIST_PROBE], env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.PIPE, text=True))
+    outs = []
+    for p in procs:
+        out, err = p.communicate(timeout=240)
+        assert p.returncode == 0, err
+        outs.append(json.loads([l for l in out.splitlines() if l.startswith("{")][0]))
+    assert sorted(o["rank"] for o in outs) == [0, 1]
+    for o in outs:
+        assert o["ws"] == 2 and o["max"] == 2.5 and o["sum"] == 3.0
+
+
+def test_reference_arm_runs_on_rank_0_only():
+    """Under a launcher with two ranks the reference arm's rank 1 exits 0
+    without work and prints nothing."""
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "64",
+                        "--steps", "1", "--warmup", "1", "--ref-iters", "5"],
+                       capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert not [l for l in r.stdout.splitlines() if l.startswith("{")]
