@@ -199,6 +199,14 @@ tl_chunk_t *tl_default_chunk(void);
  * the same from ./tea.in) */
 int tl_default_chunk_init(const tl_config_t *cfg);
 
+/* tl_test_fail_alloc -- no counterpart in the reference; a test hook for
+ * the allocation-failure paths.  Counting from this call, the nth device
+ * allocation the library makes (chunk fields, mixed-precision and warm-start
+ * buffers) reports cudaErrorMemoryAllocation without calling cudaMalloc, so
+ * the caller sees TL_ERR_ALLOC and everything allocated before it is freed.
+ * 0 disarms it.  Returns TL_ERR_ARG for nth < 0. */
+int tl_test_fail_alloc(int nth);
+
 /* tl_dot_noalloc -- no counterpart in the reference.  The dot-product
  * reduction of tea_leaf_calc_2norm (sum of a[i]*b[i]) for callers that
  * cannot let the library allocate: hosts that set up their whole
@@ -214,7 +222,9 @@ int tl_default_chunk_init(const tl_config_t *cfg);
  * cells; larger blocks are rejected with TL_ERR_ARG).  The first call on a
  * device looks up that array's address with the device current; make that
  * first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race on it and must be ordered by the caller. */
+ * that overlap on the GPU race on it and must be ordered by the caller.
+ * The looked-up address is kept for the life of the process, so do not reset
+ * a device (cudaDeviceReset) while the library is loaded. */
 int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long pitch,
                    double *result, void *stream);
 

@@ -478,6 +478,9 @@ static double *field_ptr(const ora_chunk *ch, int f) {
     case ORA_F_CP: return ch->cp;
     case ORA_F_BFP: return ch->bfp;
     case ORA_F_VOLUME: return ch->volume;
+    case ORA_F_RTEMP: return ch->rtemp;
+    case ORA_F_UTEMP: return ch->utemp;
+    case ORA_F_R_STORE: return ch->r_store;
     default: return NULL;
     }
 }

@@ -85,7 +85,8 @@ int ora_step(ora_chunk *ch, ora_step_result *res);
 /* field access in the reference layout ((x+2h) x (y+2h), x fastest) */
 enum { ORA_F_DENSITY = 1, ORA_F_ENERGY0, ORA_F_ENERGY1, ORA_F_U, ORA_F_P,
        ORA_F_SD, ORA_F_R, ORA_F_U0, ORA_F_W, ORA_F_Z, ORA_F_KX, ORA_F_KY,
-       ORA_F_MI, ORA_F_CP, ORA_F_BFP, ORA_F_VOLUME };
+       ORA_F_MI, ORA_F_CP, ORA_F_BFP, ORA_F_VOLUME, ORA_F_RTEMP, ORA_F_UTEMP,
+       ORA_F_R_STORE };
 int ora_get_field(const ora_chunk *ch, int field, double *out);
 int ora_set_field(ora_chunk *ch, int field, const double *in);
 int ora_field_pitch(const ora_chunk *ch);

@@ -3,7 +3,12 @@
  * infrastructure).  Runs a tea.in deck through the oracle and prints one JSON
  * object per line: a "step" record per timestep and a final "run" record.
  *
- *   tea_oracle <deck> [--max-steps N]
+ *   tea_oracle <deck> [--max-steps N] [--u-samples S]
+ *
+ * --u-samples S adds to every step record the solution u at an S x S lattice
+ * of interior cells (cell centres of an even S x S partition of the grid, row
+ * by row), so that a solve on another machine can be compared with this one
+ * point by point without storing whole fields.
  */
 #include "tea_oracle.h"
 
@@ -41,7 +46,14 @@ static void num(const char *key, double v) {
     else printf(", \"%s\": %.17g", key, v);
 }
 
-static void print_step(const ora_step_result *r, double wall) {
+/* the lattice of --u-samples: S points per axis at the centres of an even
+ * partition of n cells, as 0-based interior indices */
+static int sample_index(int k, int s, int n) {
+    return (int)(((2L * k + 1) * (long)n) / (2L * s));
+}
+
+static void print_step(const ora_step_result *r, double wall, const ora_chunk *ch,
+                       const ora_config *cfg, int u_samples, double *ubuf) {
     printf("{\"kind\": \"step\", \"step\": %d, \"iterations\": %d, \"ppcg_inner\": %d, "
            "\"switch_n\": %d, \"est_itc\": %d, \"wall\": %.6f",
            r->step, r->iterations, r->ppcg_inner_iters, r->switch_n, r->est_itc, wall);
@@ -52,6 +64,18 @@ static void print_step(const ora_step_result *r, double wall) {
         num("ie", r->ie);
         num("temp", r->temp);
     }
+    if (u_samples > 0 && ubuf) {
+        ora_get_field(ch, ORA_F_U, ubuf);
+        const int h = cfg->halo_depth, pitch = ora_field_pitch(ch);
+        printf(", \"u_samples\": [");
+        for (int j = 0; j < u_samples; ++j)
+            for (int i = 0; i < u_samples; ++i) {
+                const int y = h + sample_index(j, u_samples, cfg->y_cells);
+                const int x = h + sample_index(i, u_samples, cfg->x_cells);
+                printf("%s%.17g", (i | j) ? ", " : "", ubuf[(size_t)y * pitch + x]);
+            }
+        printf("]");
+    }
     printf("}\n");
     fflush(stdout);
 }
@@ -61,9 +85,11 @@ int main(int argc, char **argv) {
         fprintf(stderr, "usage: %s <deck> [--max-steps N]\n", argv[0]);
         return 2;
     }
-    int max_steps = -1;
-    for (int i = 2; i < argc; ++i)
+    int max_steps = -1, u_samples = 0;
+    for (int i = 2; i < argc; ++i) {
         if (!strcmp(argv[i], "--max-steps") && i + 1 < argc) max_steps = atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--u-samples") && i + 1 < argc) u_samples = atoi(argv[++i]);
+    }
     char *text = slurp(argv[1]);
     if (!text) {
         fprintf(stderr, "cannot read %s\n", argv[1]);
@@ -77,9 +103,15 @@ int main(int argc, char **argv) {
     }
     ora_chunk *ch = ora_chunk_new(&cfg);
     if (!ch) return 4;
+    double *ubuf = NULL;
+    if (u_samples > 0) {
+        const int h = cfg.halo_depth;
+        ubuf = (double *)malloc((size_t)(cfg.y_cells + 2 * h) * ora_field_pitch(ch) * sizeof(double));
+        if (!ubuf) return 4;
+    }
     ora_step_result r;
     ora_start(ch, &r);
-    print_step(&r, 0.0);
+    print_step(&r, 0.0, ch, &cfg, u_samples, ubuf);
     double t0 = now();
     long total_its = 0;
     int steps = 0;
@@ -87,9 +119,10 @@ int main(int argc, char **argv) {
         int done = ora_step(ch, &r);
         steps++;
         total_its += r.iterations;
-        print_step(&r, now() - t0);
+        print_step(&r, now() - t0, ch, &cfg, u_samples, ubuf);
         if (done || (max_steps > 0 && steps >= max_steps)) break;
     }
+    free(ubuf);
     double wall = now() - t0;
     printf("{\"kind\": \"run\", \"steps\": %d, \"total_iterations\": %ld, \"wall\": %.6f, "
            "\"threads\": %d, \"cells\": %ld}\n",

@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "tl_internal.cuh"
@@ -52,8 +53,24 @@ double *field_ptr(Chunk *c, int field) {
     }
 }
 
+// Failure injection for tests of the allocation-failure paths (set by
+// tl_test_fail_alloc): when the countdown reaches zero, one device
+// allocation reports cudaErrorMemoryAllocation without calling cudaMalloc.
+static std::atomic<int> g_fail_alloc_countdown{0};
+
+cudaError_t device_malloc(void **p, size_t bytes) {
+    int n = g_fail_alloc_countdown.load();
+    while (n > 0 && !g_fail_alloc_countdown.compare_exchange_weak(n, n - 1)) {
+    }
+    if (n == 1) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 static int dalloc(Chunk *c, void **p, size_t bytes) {
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = device_malloc(p, bytes);
     if (e != cudaSuccess) {
         *p = nullptr;
         return cuda_fail(e, "cudaMalloc");
@@ -261,9 +278,9 @@ int chunk_upload_coefs(Chunk *c, const double *a, const double *b, int n) {
     if (n < 0) return TL_OK;
     if (n > c->n_coefs_cap) {
         double *na = nullptr, *nb = nullptr;
-        TL_CUDA(cudaMalloc((void **)&na, (size_t)n * sizeof(double)));
-        TL_CUDA(cudaMalloc((void **)&nb, (size_t)n * sizeof(double)));
-        c->allocations.push_back(na);
+        TL_CUDA(device_malloc((void **)&na, (size_t)n * sizeof(double)));
+        c->allocations.push_back(na);  // freed with the chunk even if the next one fails
+        TL_CUDA(device_malloc((void **)&nb, (size_t)n * sizeof(double)));
         c->allocations.push_back(nb);
         c->ch_alphas = na;
         c->ch_betas = nb;
@@ -342,6 +359,33 @@ void drop_graphs(Chunk *c) {
         }
 }
 
+// Host copies of a field move as one contiguous block through a device
+// staging buffer (rows x (nx + 2h), the host layout), re-pitched by a
+// kernel: a pitched 2-D copy moves one short row at a time and runs far
+// below the host link's bandwidth.
+// to_pitched: dst[r * pitch + c] = src[r * w + c]; else the reverse
+static __global__ void k_repitch(double *__restrict__ dst, const double *__restrict__ src, int w, int pitch,
+                          int rows, bool to_pitched) {
+    for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int64_t dense = (int64_t)r * w, pitched = (int64_t)r * pitch;
+        for (int col = threadIdx.x; col < w; col += blockDim.x) {
+            if (to_pitched) dst[pitched + col] = src[dense + col];
+            else dst[dense + col] = src[pitched + col];
+        }
+    }
+}
+
+static int stage_buffer(Chunk *c, double **out) {
+    if (!c->stage) {
+        void *p;
+        int rc = dalloc(c, &p, (size_t)(c->nx + 2 * c->h) * (size_t)c->rows * sizeof(double));
+        if (rc) return rc;
+        c->stage = (double *)p;
+    }
+    *out = c->stage;
+    return TL_OK;
+}
+
 }  // namespace tl
 
 using namespace tl;
@@ -352,11 +396,34 @@ struct tl_chunk {
 
 static tl_chunk g_default = {nullptr};
 
+static int field_arg(tl_chunk_t *ch, int field, const void *host, const char *what, double **f) {
+    if (!ch || !ch->c || !host) {
+        set_error("%s: bad argument", what);
+        return TL_ERR_ARG;
+    }
+    *f = field_ptr(ch->c, field);
+    if (!*f) {
+        set_error("%s: unknown field %d", what, field);
+        return TL_ERR_ARG;
+    }
+    return TL_OK;
+}
+
+
 extern "C" {
 
 const char *tl_last_error(void) { return g_err; }
 void tl_clear_error(void) { g_err[0] = '\0'; }
 const char *tl_version(void) { return "tealeaf_gb300 1.0 (sm_103a)"; }
+
+int tl_test_fail_alloc(int nth) {
+    if (nth < 0) {
+        set_error("tl_test_fail_alloc: nth must be >= 0");
+        return TL_ERR_ARG;
+    }
+    g_fail_alloc_countdown.store(nth);
+    return TL_OK;
+}
 
 long long tl_sizeof(int which) {
     switch (which) {
@@ -407,7 +474,7 @@ int tl_start(tl_chunk_t *ch, double *vol, double *mass, double *ie, double *temp
     if (rc) return rc;
     // generate_chunk.f90 / generate_chunk_kernel_cuda.cu:50-110
     tl_state_t *sdev = nullptr;
-    TL_CUDA(cudaMalloc((void **)&sdev, sizeof(tl_state_t) * (cf.nstates > 0 ? cf.nstates : 1)));
+    TL_CUDA(device_malloc((void **)&sdev, sizeof(tl_state_t) * (cf.nstates > 0 ? cf.nstates : 1)));
     cudaMemcpyAsync(sdev, cf.states, sizeof(tl_state_t) * cf.nstates, cudaMemcpyHostToDevice, c->stream);
     rc = launch_generate(c, cf.nstates, sdev);
     cudaStreamSynchronize(c->stream);
@@ -454,38 +521,46 @@ int tl_field_summary(tl_chunk_t *ch, double *vol, double *mass, double *ie, doub
     return field_summary(ch->c, vol, mass, ie, temp);
 }
 
+
 int tl_get_field(tl_chunk_t *ch, int field, double *host) {
-    if (!ch || !ch->c || !host) {
-        set_error("tl_get_field: bad argument");
-        return TL_ERR_ARG;
-    }
+    double *f;
+    int rc = field_arg(ch, field, host, "tl_get_field", &f);
+    if (rc) return rc;
     Chunk *c = ch->c;
-    double *f = field_ptr(c, field);
-    if (!f) {
-        set_error("tl_get_field: unknown field %d", field);
-        return TL_ERR_ARG;
+    const int w = c->nx + 2 * c->h;
+    const size_t bytes = (size_t)w * (size_t)c->rows * sizeof(double);
+    if (w == c->pitch) {
+        TL_CUDA(cudaMemcpyAsync(host, f, bytes, cudaMemcpyDeviceToHost, c->stream));
+    } else {
+        double *st;
+        if ((rc = stage_buffer(c, &st))) return rc;
+        k_repitch<<<c->sms * 8, 256, 0, c->stream>>>(st, f, w, c->pitch, c->rows, false);
+        TL_CUDA(cudaGetLastError());
+        c->launches++;
+        TL_CUDA(cudaMemcpyAsync(host, st, bytes, cudaMemcpyDeviceToHost, c->stream));
     }
-    const size_t w = (size_t)(c->nx + 2 * c->h);
-    TL_CUDA(cudaMemcpy2DAsync(host, w * sizeof(double), f, (size_t)c->pitch * sizeof(double),
-                              w * sizeof(double), (size_t)c->rows, cudaMemcpyDeviceToHost, c->stream));
     TL_CUDA(cudaStreamSynchronize(c->stream));
     return TL_OK;
 }
 
 int tl_set_field(tl_chunk_t *ch, int field, const double *host) {
-    if (!ch || !ch->c || !host) {
-        set_error("tl_set_field: bad argument");
-        return TL_ERR_ARG;
-    }
+    double *f;
+    int rc = field_arg(ch, field, host, "tl_set_field", &f);
+    if (rc) return rc;
     Chunk *c = ch->c;
-    double *f = field_ptr(c, field);
-    if (!f) {
-        set_error("tl_set_field: unknown field %d", field);
-        return TL_ERR_ARG;
+    const int w = c->nx + 2 * c->h;
+    const size_t bytes = (size_t)w * (size_t)c->rows * sizeof(double);
+    if (w == c->pitch) {
+        TL_CUDA(cudaMemcpyAsync(f, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    } else {
+        double *st;
+        if ((rc = stage_buffer(c, &st))) return rc;
+        TL_CUDA(cudaMemcpyAsync(st, host, bytes, cudaMemcpyHostToDevice, c->stream));
+        k_repitch<<<c->sms * 8, 256, 0, c->stream>>>(f, st, w, c->pitch, c->rows, true);
+        TL_CUDA(cudaGetLastError());
+        c->launches++;
     }
-    const size_t w = (size_t)(c->nx + 2 * c->h);
-    TL_CUDA(cudaMemcpy2DAsync(f, (size_t)c->pitch * sizeof(double), host, w * sizeof(double),
-                              w * sizeof(double), (size_t)c->rows, cudaMemcpyHostToDevice, c->stream));
+    // the caller may reuse its buffer once this returns
     TL_CUDA(cudaStreamSynchronize(c->stream));
     return TL_OK;
 }

@@ -104,6 +104,8 @@ struct Chunk {
     double *density, *energy0, *energy1, *u, *u0, *p, *r, *w, *z, *mi, *kx, *ky, *sd,
         *rtemp, *utemp, *r_store, *cp, *bfp, *volume, *un;
     double *diag;                // diag(A), refreshed with Kx/Ky by common_init
+    double *stage;               // (rows x (nx + 2h)) contiguous copy buffer of
+                                 // tl_get_field / tl_set_field (allocated on first use)
     std::vector<void *> allocations;
     // mesh
     double *vertexx, *vertexy, *cellx, *celly, *celldx, *celldy;
@@ -168,6 +170,8 @@ inline RedCtx red_ctx(Chunk *c, int epi, bool fast) {
 }
 
 double *field_ptr(Chunk *c, int field);
+// cudaMalloc, except when tl_test_fail_alloc has armed a simulated failure
+cudaError_t device_malloc(void **p, size_t bytes);
 
 // ------------------------------------------------ kernel launch wrappers
 // (tl_kernels.cu).  `fast` selects the device-resident form: scalars are

@@ -134,7 +134,7 @@ void generate_chunk_kernel_cuda_(const int *number_of_states, const double *stat
                                           : 0;
     }
     tl_state_t *sdev = nullptr;
-    if (cudaMalloc((void **)&sdev, sizeof(tl_state_t) * st.size()) != cudaSuccess) {
+    if (device_malloc((void **)&sdev, sizeof(tl_state_t) * st.size()) != cudaSuccess) {
         set_error("generate_chunk_kernel_cuda_: cudaMalloc failed");
         return;
     }

@@ -87,7 +87,12 @@ __device__ void inner_epilogue(DevScalars *s, int epi, double tot) {
         s->in_rro = tot;
         s->in_target = s->in_target * sqrt(fabs(tot));  // in_target holds inner_eps on entry
         s->in_n = 0;
-        if (!(sqrt(fabs(tot)) > 0.0)) s->done = kConverged;
+        if (isnan(tot)) {  // a NaN start is a breakdown, not "nothing to solve"
+            s->done = kBreakdown;
+            s->n_exit = s->n;
+        } else if (!(sqrt(fabs(tot)) > 0.0)) {
+            s->done = kConverged;
+        }
         break;
     case kInW:
         s->in_pw = tot;
@@ -1267,8 +1272,8 @@ struct BodyPpUr {
 
 Mixed *mixed_of(Chunk *c) { return (Mixed *)c->mixed; }
 
-int mixed_alloc(Chunk *c) {
-    if (c->mixed) return TL_OK;
+// the FP32 state; on failure nothing of it is kept (mixed_alloc frees it)
+int mixed_alloc_fields(Chunk *c) {
     Mixed *mx = new Mixed();
     c->mixed = mx;
     const size_t n = (size_t)c->lead + (size_t)c->pitch * (size_t)c->rows + 32;
@@ -1277,7 +1282,7 @@ int mixed_alloc(Chunk *c) {
                      &mx->rtemp2};
     for (float **a : arr) {
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, n * sizeof(float));
+        cudaError_t e = device_malloc(&p, n * sizeof(float));
         if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");
         mx->allocs.push_back(p);
         TL_CUDA(cudaMemsetAsync(p, 0, n * sizeof(float), c->stream));
@@ -1286,7 +1291,7 @@ int mixed_alloc(Chunk *c) {
     mx->vtiles_x = (c->nx + kVCols - 1) / kVCols;
     mx->vtiles = mx->vtiles_x * ((c->ny + kVTileRows - 1) / kVTileRows);
     void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, sizeof(double) * (size_t)mx->vtiles + 256);
+    cudaError_t e = device_malloc(&p, sizeof(double) * (size_t)mx->vtiles + 256);
     if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");
     mx->allocs.push_back(p);
     TL_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * (size_t)mx->vtiles + 256, c->stream));
@@ -1294,11 +1299,18 @@ int mixed_alloc(Chunk *c) {
     mx->partials = (double *)((char *)p + 256);
     // the most CTAs a fused pass can have: the narrowest band, one strip per share
     const size_t fcta = (size_t)((c->nx + kFusedBandMin - 1) / kFusedBandMin) * (size_t)((c->ny + 3) / 4);
-    e = cudaMalloc(&p, sizeof(double) * fcta);
+    e = device_malloc(&p, sizeof(double) * fcta);
     if (e != cudaSuccess) return cuda_fail(e, "mixed cudaMalloc");
     mx->allocs.push_back(p);
     mx->fpartials = (double *)p;
     return TL_OK;
+}
+
+int mixed_alloc(Chunk *c) {
+    if (c->mixed) return TL_OK;
+    const int rc = mixed_alloc_fields(c);
+    if (rc) mixed_free(c);
+    return rc;
 }
 
 template <class Body>
@@ -1671,6 +1683,11 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
     int outer = 0, inner_total = 0;
     int status = TL_OK;
     while (true) {
+        if (isnan(rn)) {  // a NaN residual never meets the tests below
+            set_error("mixed solve: breakdown (NaN in the FP64 residual) after %d refinement steps", outer);
+            status = TL_ERR_BREAKDOWN;
+            break;
+        }
         if (rn < target) break;
         if (outer > 0 && rn > 0.5 * rn_prev) break;  // FP64 residual floor reached
         if (outer >= kMaxOuter || inner_total >= cf.max_iters) {

@@ -18,6 +18,10 @@
 // on a device share it and it keeps the last call's contents, so each call
 // clears the ticket counter first, and calls that overlap on the GPU (two
 // streams, or two host threads) race on it: the caller must order them.
+// The array's device address is looked up on the first call on each device
+// and kept for the life of the process, so a device must not be reset
+// (cudaDeviceReset) while this library is loaded: after a reset the module
+// reloads and the array may move.
 #include <stdint.h>
 
 #include "tl_internal.cuh"
@@ -105,9 +109,10 @@ extern "C" int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, 
         set_error("tl_dot_noalloc: bad arguments (nx=%d ny=%d pitch=%lld)", nx, ny, pitch);
         return TL_ERR_ARG;
     }
-    const long long tiles_x = (nx + kTileCols - 1) / kTileCols;
-    const long long tiles = tiles_x * ((ny + kTileRows - 1) / kTileRows);
-    if (tiles > kNoallocMaxTiles) {
+    // widened before the sums: nx, ny near INT_MAX must not overflow
+    const long long tiles_x = ((long long)nx + kTileCols - 1) / kTileCols;
+    const long long tiles = tiles_x * (((long long)ny + kTileRows - 1) / kTileRows);
+    if (tiles <= 0 || tiles > kNoallocMaxTiles) {
         set_error("tl_dot_noalloc: %d x %d cells need %lld scratch tiles; the fixed scratch holds "
                   "%d (at most %d cells)", nx, ny, tiles, kNoallocMaxTiles,
                   kNoallocMaxTiles * kTileCols * kTileRows);

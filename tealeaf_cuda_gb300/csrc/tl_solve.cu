@@ -256,8 +256,12 @@ int solve_timestep(Chunk *c, tl_solve_info_t *info) {
             if (c->first) {
                 std::vector<double> al(n + 1, 0.0), be(n + 1, 0.0);
                 if (n > 1) {
-                    TL_CUDA(cudaMemcpy(al.data(), c->cg_alphas, sizeof(double) * n, cudaMemcpyDeviceToHost));
-                    TL_CUDA(cudaMemcpy(be.data(), c->cg_betas, sizeof(double) * n, cudaMemcpyDeviceToHost));
+                    // on the chunk's own (non-blocking) stream, then wait for it
+                    TL_CUDA(cudaMemcpyAsync(al.data(), c->cg_alphas, sizeof(double) * n,
+                                            cudaMemcpyDeviceToHost, c->stream));
+                    TL_CUDA(cudaMemcpyAsync(be.data(), c->cg_betas, sizeof(double) * n,
+                                            cudaMemcpyDeviceToHost, c->stream));
+                    TL_CUDA(cudaStreamSynchronize(c->stream));
                 }
                 double emin = 0.0, emax = 0.0;
                 const int info_e = tl_calc_eigenvalues(al.data() + 1, be.data() + 1, n - 1, &emin, &emax);

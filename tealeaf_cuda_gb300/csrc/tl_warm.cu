@@ -286,7 +286,7 @@ __global__ void k_combine(Geo g, const double *__restrict__ u0, Dirs D, Coefs C,
 Warm *warm_of(Chunk *c) { return (Warm *)c->warm; }
 
 int dmalloc(std::vector<void *> &list, void **p, size_t bytes, cudaStream_t s) {
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = device_malloc(p, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "warm start cudaMalloc");
     list.push_back(*p);
     e = cudaMemsetAsync(*p, 0, bytes, s);
@@ -305,12 +305,20 @@ void free_model(Warm *w) {
     w->model = false;
 }
 
-// the per-chunk warm start state, created on first use
+// the per-chunk warm start state, created on first use; on failure nothing
+// of it is kept
+int warm_state_fields(Chunk *c, Warm **out);
 int warm_state(Chunk *c, Warm **out) {
     if (c->warm) {
         *out = warm_of(c);
         return TL_OK;
     }
+    const int rc = warm_state_fields(c, out);
+    if (rc) warm_free(c);
+    return rc;
+}
+
+int warm_state_fields(Chunk *c, Warm **out) {
     Warm *w = new Warm();
     c->warm = w;
     const size_t bytes = sizeof(double) * c->alloc_elems;
@@ -551,6 +559,13 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
         D.d[D.n++] = w->dnet;
         for (int j = 0; j < w->nhist; ++j) D.d[D.n++] = w->hist[(w->cur - j + kHist) % kHist];
         if ((rc = gram_project(c, w, D, &C, &gain))) return rc;
+        if (!(gain >= gh)) {
+            // the network's direction is unusable (not finite, e.g. a model
+            // of NaNs) or adds nothing: fall back to the history start
+            D = H;
+            C = CH;
+            gain = gh;
+        }
     }
     if ((rc = chunk_sync_scalars(c))) return rc;
     const double rr0 = c->sc_host->sum[0];

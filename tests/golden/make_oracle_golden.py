@@ -1,13 +1,25 @@
 """Golden fixtures of the CPU oracle for the configurations the reference
-publishes nothing for: CG + jac_diag, CG + jac_block, Chebyshev after 20 CG
-steps and PPCG with 10 inner steps on the standard deck (BASELINE config 2),
-at 1024^2 for 20 timesteps and at 4096^2 for the first timestep.
+publishes nothing for, on the standard deck (the 4096^2 configuration of the
+scope: 20 timesteps each of CG + jac_diag, CG + jac_block, Chebyshev after
+20 CG steps, and PPCG with 10 inner steps and block-Jacobi, the headline
+method's preconditioner), at 1024^2 and 4096^2.
+
+Chebyshev runs at tl_eps 1e-10: at 1e-15 it measures the true residual,
+whose FP64 floor lies above 1e-15 * ||r_0|| on these grids, so every step
+would run to tl_max_iters and its iteration counts would pin nothing.
+
+Every step record also carries u at a 16 x 16 lattice of interior cells
+(`u_samples`, tea_oracle --u-samples), against which the mixed-precision
+solves report their per-timestep pointwise error.
 
 The oracle is pinned against the reference's own benchmark outputs
 (tests/test_oracle_golden.py); these fixtures let the GPU tests compare
 against it at sizes where rerunning the oracle inside a test would take too
-long.  Usage:
-    python tests/golden/make_oracle_golden.py [--sizes 1024,4096] [--threads N]
+long (4096^2 x 20 timesteps is about an hour a method on 8 cores).  Usage:
+    python tests/golden/make_oracle_golden.py [--sizes 1024,4096]
+        [--methods cg_jac_diag,...] [--threads N]
+Methods already present in a fixture file are kept; delete an entry to
+regenerate it.
 """
 import argparse
 import json
@@ -24,35 +36,39 @@ METHODS = {
     "cg_jac_diag": {"tl_use_cg": True, "tl_preconditioner_type": "jac_diag"},
     "cg_jac_block": {"tl_use_cg": True, "tl_preconditioner_type": "jac_block"},
     "chebyshev": {"tl_use_cg": False, "tl_use_chebyshev": True, "tl_ch_cg_presteps": 20,
-                  "tl_preconditioner_type": "none"},
-    "ppcg": {"tl_use_cg": False, "tl_use_ppcg": True, "tl_ppcg_inner_steps": 10,
-             "tl_preconditioner_type": "none"},
+                  "tl_preconditioner_type": "none", "tl_eps": 1.0e-10},
+    "ppcg_jac_block": {"tl_use_cg": False, "tl_use_ppcg": True, "tl_ppcg_inner_steps": 10,
+                       "tl_preconditioner_type": "jac_block"},
 }
-STEPS = {1024: 20, 4096: 1}
+STEPS = 20
+U_SAMPLES = 16
 
 
-def deck_for(n, method):
-    return decks.make_deck(n=n, end_step=STEPS[n], **METHODS[method])
+def deck_for(n, method, steps=STEPS):
+    return decks.make_deck(n=n, end_step=steps, **METHODS[method])
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sizes", default="1024,4096")
+    ap.add_argument("--methods", default=",".join(METHODS))
     ap.add_argument("--threads", type=int, default=None)
     args = ap.parse_args()
     for n in [int(x) for x in args.sizes.split(",")]:
         path = os.path.join(HERE, f"oracle_config2_{n}.json")
         out = {"source": "oracle/ (CPU restatement), tests/golden/make_oracle_golden.py",
-               "n": n, "steps": STEPS[n], "methods": {}}
+               "n": n, "u_samples": U_SAMPLES, "methods": {}}
         if os.path.exists(path):
             out = json.load(open(path))
-        for m in METHODS:
+        for m in args.methods.split(","):
             if m in out["methods"]:
                 continue
-            steps, run = run_deck(deck_for(n, m), threads=args.threads)
-            out["methods"][m] = {"deck_params": METHODS[m], "steps": steps, "wall": run["wall"],
-                                 "threads": run["threads"]}
-            json.dump(out, open(path, "w"), indent=1)
+            steps, run = run_deck(deck_for(n, m), threads=args.threads, u_samples=U_SAMPLES)
+            out["methods"][m] = {"deck_params": METHODS[m], "end_step": STEPS, "steps": steps,
+                                 "wall": run["wall"], "threads": run["threads"]}
+            with open(path + ".tmp", "w") as f:
+                json.dump(out, f, indent=1)
+            os.replace(path + ".tmp", path)
             print(f"{n} {m}: {[s['iterations'] for s in steps[1:]]} in {run['wall']:.1f}s", flush=True)
 
 

@@ -11,7 +11,8 @@ _lib = None
 _D = C.POINTER(C.c_double)
 
 FIELD = {"density": 1, "energy0": 2, "energy1": 3, "u": 4, "p": 5, "sd": 6, "r": 7, "u0": 8,
-         "w": 9, "z": 10, "kx": 11, "ky": 12, "mi": 13, "cp": 14, "bfp": 15, "volume": 16}
+         "w": 9, "z": 10, "kx": 11, "ky": 12, "mi": 13, "cp": 14, "bfp": 15, "volume": 16,
+         "rtemp": 17, "utemp": 18, "r_store": 19}
 
 
 def lib():

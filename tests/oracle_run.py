@@ -16,8 +16,10 @@ def build_oracle():
     return ORACLE_BIN
 
 
-def run_deck(deck_text, max_steps=None, threads=None):
-    """Run a deck through the oracle; returns (step records, run record)."""
+def run_deck(deck_text, max_steps=None, threads=None, u_samples=0):
+    """Run a deck through the oracle; returns (step records, run record).
+    With u_samples S every step record also holds u at an S x S lattice of
+    interior cells (`u_samples`, see sample_cells)."""
     build_oracle()
     with tempfile.NamedTemporaryFile("w", suffix=".in", delete=False) as f:
         f.write(deck_text)
@@ -26,6 +28,8 @@ def run_deck(deck_text, max_steps=None, threads=None):
         cmd = [ORACLE_BIN, path]
         if max_steps:
             cmd += ["--max-steps", str(max_steps)]
+        if u_samples:
+            cmd += ["--u-samples", str(u_samples)]
         env = dict(os.environ)
         if threads:
             env["OMP_NUM_THREADS"] = str(threads)
@@ -36,3 +40,9 @@ def run_deck(deck_text, max_steps=None, threads=None):
     steps = [r for r in recs if r["kind"] == "step"]
     run = [r for r in recs if r["kind"] == "run"][0]
     return steps, run
+
+
+def sample_cells(n, s):
+    """0-based interior indices of the oracle's --u-samples lattice along an
+    axis of n cells: the centres of an even partition into s parts."""
+    return [((2 * k + 1) * n) // (2 * s) for k in range(s)]

@@ -112,9 +112,9 @@ def test_calls_without_a_chunk_fail_with_status():
 
 
 def test_integration_c_example_compiles_and_links(tmp_path):
-    """The C usage of INTEGRATION.md (deck text -> config -> chunk -> start ->
-    timestep -> field summary) compiles as C11 against the public header and
-    links against the library (it is not run: that needs a GPU)."""
+    """The C usage shown to integrators (deck text -> config -> chunk ->
+    start -> timestep -> field summary) compiles as C11 against the public
+    header and links against the library (it is not run: that needs a GPU)."""
     import shutil
     import subprocess
     gcc = shutil.which("gcc")
@@ -141,3 +141,11 @@ int main(void) { return run("*tea\nstate 1 density=100.0 energy=0.0001\nx_cells=
     r = subprocess.run([gcc, "-std=c11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
                         "-L", build, "-ltealeaf_gb300", "-o", str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_alloc_failure_hook_checks_its_argument():
+    """tl_test_fail_alloc only arms a counter on the host (no GPU call)."""
+    lib = tl.load()
+    assert lib.tl_test_fail_alloc(-1) == tl.TL_ERR_ARG
+    assert "nth" in tl.last_error()
+    assert lib.tl_test_fail_alloc(0) == tl.TL_OK

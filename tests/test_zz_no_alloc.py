@@ -50,11 +50,13 @@ def test_dot_noalloc_matches_calc_2norm_twice():
         expect[which] = out.value
     hd = cfg.halo_depth
     shape = (ny + 2 * hd, nx + 2 * hd)
-    fields = {}
+    fields, independent = {}, {}
     for which, name in ((0, "u0"), (1, "r")):
         host = np.empty(shape, dtype=np.float64)
         assert lib.tl_get_field(h, tl.FIELDS[name], host.ctypes.data) == 0
         fields[which] = torch.from_numpy(host).to("cuda:0")  # caller-owned device memory
+        inner = host[hd:hd + ny, hd:hd + nx].ravel()
+        independent[which] = float(np.dot(inner, inner))
     pitch = shape[1]
     out = torch.full((4,), -1.0, dtype=torch.float64, device="cuda:0")
     stream = torch.cuda.current_stream().cuda_stream
@@ -70,6 +72,8 @@ def test_dot_noalloc_matches_calc_2norm_twice():
     for call in range(2):
         for which in (0, 1):
             assert got[2 * call + which] == pytest.approx(expect[which], rel=1e-12), (call, which)
+            # and against a sum made without the library at all
+            assert got[2 * call + which] == pytest.approx(independent[which], rel=1e-12), (call, which)
     # the second call must not see the first call's leftovers
     assert got[0] == got[2] and got[1] == got[3]
 
