@@ -25,9 +25,15 @@ Legs (one JSON line):
              between steps.
   plain      K solves of FP64 CG + jac_diag from a fresh start (timed the
              same way; gives the work count and the baseline time).
+Each timed step is a solve plus its field summary, and the summaries of the
+two methods are compared timestep by timestep.
   roofline   K more headline solves with per-kernel CUDA events (eager
              launches); the dominant kernel's algorithmic bytes per launch /
-             its mean launch time, against the measured HBM copy bandwidth.
+             its mean launch time, against the measured HBM copy bandwidth;
+             and the three largest kernels each against its own bound (HBM,
+             or the FP64 pipe at a measured DGEMM FMA rate).
+  prev       (learned warm start only) K solves of the same method started
+             from the increment history alone, to show the network's gain.
   e2e        K more headline solves through the C-ABI with host buffers:
              density and energy copied host->device before and energy copied
              back after every solve, inside the timed region.
@@ -106,6 +112,17 @@ TRAFFIC_PER_CELL = {
     "cg_w": 39.6,             # BodyCgW at 4096^2: 545.5 + 119.4 MB
 }
 
+
+# FP64 instructions per interior cell of the kernels whose bound is GB300's
+# FP64 pipe rather than HBM (DFMA, DMUL and DADD each take one issue of the
+# pipe): the operator of tea_leaf_common.cuknl:28-34 as 6 instructions
+# (DMUL, DFMA, DMUL, DFMA, DFMA, DADD), or 5 in the mixed-precision outer
+# pass (DMUL + 4 DFMA), plus one DFMA per dot product
+FP64_INSTR_PER_CELL = {
+    "ppcg_w_zr": 7,   # 5-instruction operator, p.w, r.z
+    "cg_w": 7,        # 6-instruction operator, p.w
+    "residual": 8,    # 6-instruction operator, u0 - Au, r.r
+}
 
 INNER_STEPS = 10  # tl_ppcg_inner_steps of the workload's deck
 FUSED_STEPS = 5   # FP32 inner steps per fused pass (the library's default)
@@ -310,17 +327,58 @@ def run_reference(args):
 
 # ------------------------------------------------------------------- ours
 def timed_solves(ch, stream, steps, torch):
-    """`steps` solves timed with CUDA events on the library stream; returns
-    (total ms, per-step ms, per-step solve infos)"""
+    """`steps` timesteps (solve + field summary, the loop body of
+    diffuse.f90:43-101) timed with CUDA events on the library stream;
+    returns (total ms, per-step ms, per-step solve infos, per-step field
+    summaries)"""
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    infos = []
+    infos, sums = [], []
     evs[0].record(stream)
     for k in range(steps):
         infos.append(ch.timestep())
+        sums.append(ch.field_summary())
         evs[k + 1].record(stream)
     evs[-1].synchronize()
     per = [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)]
-    return evs[0].elapsed_time(evs[-1]), per, infos
+    return evs[0].elapsed_time(evs[-1]), per, infos, sums
+
+
+def fp64_fma_peak(torch, device):
+    """measured FP64 FMA rate of this GPU (FMA/s): a cuBLAS DGEMM of
+    4096^3 (2 n^3 flops = n^3 FMAs), best of 5 after a warm-up"""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=device)
+    b = torch.randn(n, n, dtype=torch.float64, device=device)
+    torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    return n ** 3 / (best * 1e-3)
+
+
+def kernel_roofline(name, st, cells, precond, hbm_peak, fp64_peak):
+    """one kernel's roofline entry from its launch count and total ms: the
+    HBM fraction (algorithmic bytes / mean launch time) and, for the
+    FP64-pipe kernels, the FP64 instruction fraction; `bound` is the larger"""
+    launch_ms = st["ms"] / st["launches"]
+    out = {"kernel": name, "launches": st["launches"], "launch_ms": launch_ms}
+    bpc = bytes_per_cell(name, precond)
+    if bpc:
+        gbs = bpc * cells / (launch_ms * 1e-3) / 1e9
+        out.update({"bytes_per_cell": bpc, "hbm_gbs": gbs, "hbm_frac": gbs / hbm_peak})
+    ipc = FP64_INSTR_PER_CELL.get(name)
+    if ipc and fp64_peak:
+        rate = ipc * cells / (launch_ms * 1e-3)
+        out.update({"fp64_instr_per_cell": ipc, "fp64_instr_per_s": rate, "fp64_frac": rate / fp64_peak})
+    out["bound"] = "fp64" if out.get("fp64_frac", 0.0) > out.get("hbm_frac", 0.0) else "hbm"
+    return out
 
 
 def load_model(ch, lib, path):
@@ -367,12 +425,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     launches0 = ch.kernel_launches
     with ClockSampler(local) as clk:
-        ms, per_ms, infos = timed_solves(ch, stream, K, torch)
+        ms, per_ms, infos, sums_h = timed_solves(ch, stream, K, torch)
     torch.cuda.synchronize()
     barrier(ws)
     launches = ch.kernel_launches - launches0
     clocks = clk.summary()
-    summary_h = ch.field_summary()
+    summary_h = sums_h[-1]
     its_h = [i["iterations"] for i in infos]
 
     # ---- roofline: per-kernel CUDA events over the same K timesteps
@@ -391,6 +449,7 @@ def run_ours(args):
             kernels[name.value.decode()] = {"launches": cnt.value, "ms": kms.value}
         k += 1
     lib.tl_set_profiling(ch._h, 0)
+    fp64_peak = fp64_fma_peak(torch, f"cuda:{local}")
     total_kms = sum(v["ms"] for v in kernels.values()) or 1.0
     dom = max(kernels, key=lambda x: kernels[x]["ms"])
     dom_launch_ms = kernels[dom]["ms"] / kernels[dom]["launches"]
@@ -411,7 +470,13 @@ def run_ours(args):
                 "bytes_per_cell": bpc, "launch_ms": dom_launch_ms,
                 "kernel_share": {k2: round(v["ms"] / total_kms, 4) for k2, v in
                                  sorted(kernels.items(), key=lambda kv: -kv[1]["ms"])},
-                "measured_over": f"timesteps 1..{K}, eager launches with per-kernel CUDA events"}
+                "measured_over": f"timesteps 1..{K}, eager launches with per-kernel CUDA events",
+                # the three kernels with the largest share, each against its own bound:
+                # HBM (measured copy rate) or the FP64 pipe (measured DGEMM FMA rate)
+                "top_kernels": [kernel_roofline(k2, kernels[k2], cells, args.precond, peak, fp64_peak)
+                                for k2 in sorted(kernels, key=lambda x: -kernels[x]["ms"])[:3]],
+                "fp64_peak": {"value": fp64_peak, "unit": "FP64 FMA/s",
+                              "how": "torch.matmul float64 4096^3 (cuBLAS DGEMM), best of 5, n^3 FMAs"}}
 
     # ---- e2e: the state lives on the host; every timestep uploads density
     # and energy from pinned buffers, solves and reads energy back
@@ -436,6 +501,21 @@ def run_ours(args):
     e2e_s = allreduce_max(time.perf_counter() - t0, ws, local)
     ch.close()
 
+    # ---- the same method started from the increment history alone (no
+    # network), for the network's gain over the method without it
+    prev_ms = prev_per_ms = prev_its = None
+    if args.warm == "learned":
+        qcfg = tl.parse_deck(make_deck(n, solver=args.solver, precond=args.precond, precision=args.precision,
+                                       warm="prev"))
+        qcfg.cuda_device = local
+        qch = tl.Chunk(qcfg)
+        qstream = torch.cuda.ExternalStream(lib.tl_chunk_stream(qch._h), device=local)
+        qch.start()
+        torch.cuda.synchronize()
+        prev_ms, prev_per_ms, qinfos, _ = timed_solves(qch, qstream, K, torch)
+        prev_its = [i["iterations"] for i in qinfos]
+        qch.close()
+
     # ---------------- plain FP64 CG + jac_diag on the same timesteps
     pcfg = tl.parse_deck(make_deck(n))
     pcfg.cuda_device = local
@@ -444,8 +524,8 @@ def run_ours(args):
     pch.start()
     barrier(ws)
     torch.cuda.synchronize()
-    pms, pper_ms, pinfos = timed_solves(pch, pstream, K, torch)
-    summary_p = pch.field_summary()
+    pms, pper_ms, pinfos, sums_p = timed_solves(pch, pstream, K, torch)
+    summary_p = sums_p[-1]
     pch.close()
     its_p = [i["iterations"] for i in pinfos]
 
@@ -455,6 +535,7 @@ def run_ours(args):
     e2e = {"value": work / e2e_s, "unit": "plain-CG cell-iters/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / K, "iterations_per_step": e2e_its}
     rel = [abs(a - b) / abs(b) if b else abs(a) for a, b in zip(summary_h, summary_p)]
+    rel_steps = [max(abs(a - b) / abs(b) if b else abs(a) for a, b in zip(x, y)) for x, y in zip(sums_h, sums_p)]
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -485,9 +566,19 @@ def run_ours(args):
                        "plain_time_to_solution_ms": pper_ms,
                        "time_to_solution_speedup_vs_plain": pms / ms,
                        "field_summary_rel_diff_vs_plain": max(rel),
+                       "field_summary_rel_diff_vs_plain_per_step": rel_steps,
+                       "prev_start_time_to_solution_ms": prev_per_ms,
+                       "prev_start_iterations_per_step": prev_its,
+                       "learned_over_prev_speedup": (prev_ms / ms) if prev_ms else None,
                        "warm_used": [i.get("warm_used") for i in infos],
                        "l2": "fields larger than L2, no flush",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
+            # the speed-up over the reference arm is the product of the
+            # method's gain (same GPU) and the GPU's over the CPU (same method)
+            "ratio_split": {
+                "method_speedup_vs_plain_gpu": pms / ms,
+                "plain_gpu_cell_iters_per_s": work / (pms * 1e-3),
+                "plain_gpu_over_cpu": (work / (pms * 1e-3)) / cpu["value"] if cpu else None},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": launches,
         }

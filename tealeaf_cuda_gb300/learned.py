@@ -90,6 +90,48 @@ def random_deck(seed, n, steps, **kw):
     return deck_text(random_states(seed), n, steps, **kw)
 
 
+# the five-state problem of the reference's benchmark decks (tea_bm_*.in)
+STANDARD_STATES = [
+    {"index": 1, "density": 100.0, "energy": 0.0001},
+    {"index": 2, "density": 0.1, "energy": 25.0, "geometry": "rectangle",
+     "xmin": 0.0, "xmax": 1.0, "ymin": 1.0, "ymax": 2.0},
+    {"index": 3, "density": 0.1, "energy": 0.1, "geometry": "rectangle",
+     "xmin": 1.0, "xmax": 6.0, "ymin": 1.0, "ymax": 2.0},
+    {"index": 4, "density": 0.1, "energy": 0.1, "geometry": "rectangle",
+     "xmin": 5.0, "xmax": 6.0, "ymin": 1.0, "ymax": 8.0},
+    {"index": 5, "density": 0.1, "energy": 0.1, "geometry": "rectangle",
+     "xmin": 5.0, "xmax": 10.0, "ymin": 7.0, "ymax": 8.0},
+]
+
+
+def deck_for(spec, n, steps, **kw):
+    """"standard" (the benchmark deck) or a random deck's seed"""
+    if spec == "standard":
+        return deck_text(STANDARD_STATES, n, steps, **kw)
+    return random_deck(int(spec), n, steps, **kw)
+
+
+def parse_decks(text):
+    """"standard,20000-20019" -> ["standard", 20000, ..., 20019]"""
+    out = []
+    for part in text.split(","):
+        if part == "standard":
+            out.append(part)
+        elif "-" in part:
+            lo, hi = (int(x) for x in part.split("-"))
+            out += list(range(lo, hi + 1))
+        else:
+            out.append(int(part))
+    return out
+
+
+# algorithmic HBM bytes per cell of one outer iteration of the headline
+# method's PPCG phase (mixed precision, two fused passes of 5 inner steps):
+# w = Ap with p.w, r.z and r_store (64), rrn (24), u and p (40), r (24),
+# and the two fused passes (36 each)
+PPCG_OUTER_BYTES_PER_CELL = 64 + 24 + 40 + 24 + 2 * 36
+
+
 # ---------------------------------------------------------------- model
 
 def param_count():
@@ -372,16 +414,17 @@ def evaluate(params, seeds, n, steps, precond="jac_diag"):
     return rows
 
 
-def compare_methods(params, seeds, n, steps):
+def compare_methods(params, seeds, n, steps, warm="learned"):
     """Plain FP64 CG + jac_diag from u = u^n against the headline method
     (PPCG + block-Jacobi, 10 FP32 inner steps under the FP64 outer solve,
-    learned warm start) on seeded random decks: per timestep the
-    iterations, the solve's wall time and the field summaries."""
+    warm start `warm`) on the given decks ("standard" or a random deck's
+    seed): per timestep the iterations (outer, and PPCG inner), the solve's
+    wall time and the field summaries' relative difference."""
     from . import PREC_JAC_BLOCK, PRECISION_MIXED, SOLVER_PPCG
     lib = load()
     rows = []
     for seed in seeds:
-        deck = random_deck(seed, n, steps)
+        deck = deck_for(seed, n, steps)
         out = {}
         for name in ("plain", "headline"):
             cfg = parse_deck(deck)
@@ -390,22 +433,28 @@ def compare_methods(params, seeds, n, steps):
                 cfg.precond = PREC_JAC_BLOCK
                 cfg.ppcg_inner_steps = 10
                 cfg.precision = PRECISION_MIXED
-                cfg.warm_start = WARM["learned"]
+                cfg.warm_start = WARM[warm]
             recs = []
             with Chunk(cfg) as ch:
                 ch.start()
-                if name == "headline":
+                if name == "headline" and warm == "learned":
                     p = np.ascontiguousarray(params, dtype=np.float32)
                     assert lib.tl_set_warm_start_model(ch._h, C.c_void_p(p.ctypes.data), p.size) == 0
                 for _ in range(steps):
                     info = ch.timestep()
-                    recs.append((info["iterations"], info["seconds"], ch.field_summary()))
+                    assert info["status"] == 0, (seed, name, info["status"])
+                    recs.append((info["iterations"], info["seconds"], ch.field_summary(),
+                                 info["ppcg_inner_iters"]))
             out[name] = recs
+        hs = [r[1] for r in out["headline"]]
+        outer = [r[0] for r in out["headline"]]
         rows.append({"seed": seed,
                      "plain_iters": [r[0] for r in out["plain"]],
-                     "headline_iters": [r[0] for r in out["headline"]],
+                     "headline_iters": outer,
+                     "headline_inner_iters": [r[3] for r in out["headline"]],
                      "plain_seconds": [r[1] for r in out["plain"]],
-                     "headline_seconds": [r[1] for r in out["headline"]],
+                     "headline_seconds": hs,
+                     "headline_hbm_gbs_estimate": n * n * sum(outer) * PPCG_OUTER_BYTES_PER_CELL / sum(hs) / 1e9,
                      "summary_rel_diff": [max(abs(a - b) / abs(b) for a, b in zip(h[2], q[2]))
                                           for h, q in zip(out["headline"], out["plain"])]})
     return rows
@@ -453,18 +502,23 @@ def main(argv=None):
     e.add_argument("--report", default=None)
     m = sub.add_parser("compare")
     m.add_argument("--model", required=True)
-    m.add_argument("--seeds", default="20000-20002")
+    m.add_argument("--decks", "--seeds", dest="decks", default="20000-20002",
+                   help='"standard" and/or seed ranges, e.g. standard,20000-20019')
     m.add_argument("--n", type=int, default=8192)
     m.add_argument("--steps", type=int, default=5)
+    m.add_argument("--warm", default="learned", choices=["none", "prev", "learned"])
     m.add_argument("--report", default=None)
     a = ap.parse_args(argv)
     if a.cmd == "compare":
-        lo, hi = (int(x) for x in a.seeds.split("-"))
-        rows = compare_methods(load_model(a.model), list(range(lo, hi + 1)), a.n, a.steps)
+        rows = compare_methods(load_model(a.model), parse_decks(a.decks), a.n, a.steps, warm=a.warm)
         tp = sum(sum(r["plain_seconds"]) for r in rows)
         th = sum(sum(r["headline_seconds"]) for r in rows)
-        rep = {"n": a.n, "steps": a.steps, "seeds": a.seeds, "plain_seconds": tp, "headline_seconds": th,
-               "speedup": tp / th, "max_summary_rel_diff": max(max(r["summary_rel_diff"]) for r in rows),
+        rep = {"n": a.n, "steps": a.steps, "decks_run": a.decks, "warm": a.warm,
+               "plain_seconds": tp, "headline_seconds": th, "speedup": tp / th,
+               "plain_iterations": sum(sum(r["plain_iters"]) for r in rows),
+               "headline_outer_iterations": sum(sum(r["headline_iters"]) for r in rows),
+               "headline_inner_iterations": sum(sum(r["headline_inner_iters"]) for r in rows),
+               "max_summary_rel_diff": max(max(r["summary_rel_diff"]) for r in rows),
                "decks": rows}
         print(json.dumps({k: v for k, v in rep.items() if k != "decks"}))
         if a.report:
