@@ -571,6 +571,8 @@ def run_ours(args):
                        "prev_start_iterations_per_step": prev_its,
                        "learned_over_prev_speedup": (prev_ms / ms) if prev_ms else None,
                        "warm_used": [i.get("warm_used") for i in infos],
+                       "warm_net_share": [i.get("warm_net_share") for i in infos],
+                       "warm_ratio": [i.get("warm_ratio") for i in infos],
                        "l2": "fields larger than L2, no flush",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             # the speed-up over the reference arm is the product of the

@@ -138,6 +138,9 @@ typedef struct tl_solve_info {
     double seconds;               /* wall time of the solve on the host      */
     int warm_used;                /* warm start taken (1) or u = u^n (0)     */
     double warm_ratio;            /* its residual / the plain start's        */
+    double warm_net_share;        /* learned: the network direction's share of
+                                     the start's energy decrease (0 when it
+                                     was not consulted)                      */
 } tl_solve_info_t;
 
 typedef struct tl_chunk tl_chunk_t;
@@ -262,6 +265,14 @@ int tl_warm_start_features(tl_chunk_t *ch, float *dst);
  * 3: out = res + conv(in) (data gradient, weights from tl_nn_pack's wb). */
 int tl_nn_conv(int mode, int cin, int coutp, const void *in, const void *w, const float *bias,
                const void *res, void *out, void *pre, float *outf, int B, int H, int W, void *stream);
+/* which kernel tl_nn_conv runs: tcgen05 != 0 (the default) the
+ * 5th-generation tensor-core kernel (tcgen05.mma, tensor-memory
+ * accumulators, 128-pixel tiles), 0 the warp-level mma.sync kernel */
+int tl_nn_set_conv_kernel(int tcgen05);
+/* TL_OK, or TL_ERR_CUDA (and clears the flag) if a tcgen05 conv since the
+ * last call gave up waiting for its tensor-core result (synchronises with
+ * the device; the result of that conv is not written) */
+int tl_nn_conv_status(void);
 int tl_nn_gelu_backward(const void *dh, const void *pre, void *dpre, int C, int B, int H, int W,
                         void *stream);
 long long tl_nn_wgrad_partial_floats(int cin, int coutp, int B, int H, int W, int groups_per_cta);

@@ -59,7 +59,7 @@ class SolveInfo(C.Structure):
                 ("error_ratio", C.c_double), ("exact_error_ratio", C.c_double),
                 ("eigmin", C.c_double), ("eigmax", C.c_double), ("rx", C.c_double),
                 ("ry", C.c_double), ("seconds", C.c_double), ("warm_used", C.c_int),
-                ("warm_ratio", C.c_double)]
+                ("warm_ratio", C.c_double), ("warm_net_share", C.c_double)]
 
 
 class StepRecord(C.Structure):

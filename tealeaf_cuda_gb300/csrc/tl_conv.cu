@@ -125,6 +125,235 @@ __global__ void __launch_bounds__(128) k_conv(const bf16 *__restrict__ in, const
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same convolution on the 5th-generation tensor cores (tcgen05): a CTA
+// of 4 warps computes a tile of 128 pixels of one row (M = 128) for all
+// COUTP output channels (N), accumulating in tensor memory.
+//
+// Shared memory holds, per kernel row dy, the 130 input pixels the tile's
+// three taps dx = 0, 1, 2 read, in the K-major no-swizzle layout of the MMA
+// operands: 16-byte core-matrix rows (one pixel, 8 channels), the pixels of
+// an 8-channel chunk contiguous (16 bytes apart) and the chunks kChunkA bytes
+// apart.  The A operand of tap (dy, dx) and 16-channel step kk is that block
+// shifted by dx pixels: start + dx * 16, core matrices 128 bytes apart along
+// M (SBO) and kChunkA along K (LBO).  The weights [tap][cout][cin] sit in the
+// same layout (cout rows 16 bytes apart, chunks 16 * COUTP apart).  One
+// thread issues the 9 * CIN / 16 MMAs (M 128, N COUTP, K 16, BF16 in, FP32
+// accumulate) and commits them to an mbarrier; each warp then reads its 32
+// TMEM lanes (one pixel a lane, one channel a column) and runs the epilogue
+// of k_conv.
+constexpr int kTcPix = 128;               // pixels of a tile (MMA M)
+constexpr int kTcRow = kTcPix + 2;        // input pixels a kernel row reads
+constexpr int kChunkA = kTcRow * 16;      // bytes between 8-channel chunks of A
+constexpr int kTmemCols = 32;             // accumulator columns allocated (>= COUTP)
+constexpr long long kTcWaitCycles = 2000000000LL;  // ~1 s: the MMA wait gives up after this
+
+// set by a tcgen05 conv whose MMA completion wait ran out (read and cleared
+// by tl_nn_conv_status)
+__device__ int g_conv_tc_error;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// shared-memory matrix descriptor: no swizzle, version 1 (bits 46-47)
+__device__ __forceinline__ uint64_t mma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16
+// A and B (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t mma_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait on phase `parity` of an mbarrier: false if it ran out
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kTcWaitCycles) return false;
+    return true;
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_load(uint32_t taddr, float (&v)[N]);
+
+template <>
+__device__ __forceinline__ void tmem_load<32>(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <>
+__device__ __forceinline__ void tmem_load<16>(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+        "[%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+
+template <int CIN, int COUTP, int MODE>
+__global__ void __launch_bounds__(128) k_conv_tc(const bf16 *__restrict__ in, const bf16 *__restrict__ wt,
+                                                 const float *__restrict__ bias,
+                                                 const bf16 *__restrict__ res, bf16 *__restrict__ out,
+                                                 bf16 *__restrict__ pre, float *__restrict__ outf, int B,
+                                                 int H, int W) {
+    static_assert(CIN % 16 == 0 && COUTP % 16 == 0 && COUTP <= kTmemCols, "conv shape");
+    constexpr int CA = CIN / 8;                    // 8-channel chunks of a pixel
+    constexpr int CHUNK_B = COUTP * 16;            // bytes between chunks of the weights
+    constexpr int A_BYTES = 3 * CA * kChunkA;      // three kernel rows
+    constexpr int B_BYTES = 9 * CA * CHUNK_B;      // nine taps
+    __shared__ __align__(1024) unsigned char sa[A_BYTES];
+    __shared__ __align__(1024) unsigned char sb[B_BYTES];
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (W + kTcPix - 1) / kTcPix;
+    const long long task = blockIdx.x;  // (b, y, tile)
+    const int b = (int)(task / ((long long)H * tiles_x));
+    const int rem = (int)(task % ((long long)H * tiles_x));
+    const int y = rem / tiles_x, x0 = (rem % tiles_x) * kTcPix;
+    const long long Wp = W + 2;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_addr(&tmem_slot)),
+                     "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)));
+        // the tensor cores arrive on it: make the initialisation visible to them
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // A: padded input rows y + dy, pixels x0 .. x0 + 129, 16 bytes a load;
+    // pixels past the padded row read as zero (partial last tile)
+    const bf16 *img = in + (long long)b * (H + 2) * Wp * CIN;
+    for (int k = tid; k < 3 * kTcRow * CA; k += 128) {
+        const int c = k % CA, j = (k / CA) % kTcRow, dy = k / (CA * kTcRow);
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (x0 + j < Wp) v = *reinterpret_cast<const uint4 *>(img + ((long long)(y + dy) * Wp + x0 + j) * CIN + 8 * c);
+        *reinterpret_cast<uint4 *>(sa + (dy * CA + c) * kChunkA + j * 16) = v;
+    }
+    // B: weights [tap][cout][cin]
+    for (int k = tid; k < 9 * COUTP * CA; k += 128) {
+        const int c = k % CA, co = (k / CA) % COUTP, tap = k / (CA * COUTP);
+        const uint4 v = *reinterpret_cast<const uint4 *>(wt + ((long long)tap * COUTP + co) * CIN + 8 * c);
+        *reinterpret_cast<uint4 *>(sb + (tap * CA + c) * CHUNK_B + co * 16) = v;
+    }
+    // the MMAs read shared memory through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t bar = smem_addr(&mbar);
+    if (tid == 0) {
+        constexpr uint32_t idesc = mma_idesc(kTcPix, COUTP);
+        const uint32_t a0 = smem_addr(sa), b0 = smem_addr(sb);
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;
+#pragma unroll
+            for (int kk = 0; kk < CIN / 16; ++kk) {
+                const uint64_t ad = mma_desc(a0 + (dy * CA + 2 * kk) * kChunkA + dx * 16, kChunkA, 128);
+                const uint64_t bd = mma_desc(b0 + (tap * CA + 2 * kk) * CHUNK_B, CHUNK_B, 128);
+                const uint32_t acc = (tap | kk) != 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                     : "memory");
+    }
+    // warp-uniform outcome: tcgen05.ld below is executed by whole warps
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(bar, 0));
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) {
+        // the accumulator never became ready: flag it, wait once more
+        // (bounded) for the MMAs in flight, release the columns and leave
+        if (lane == 0) atomicExch(&g_conv_tc_error, 1);
+        mbar_wait_bounded(bar, 0);
+    } else {
+        // warp w holds TMEM lanes 32w..32w+31: pixel m = 32 w + lane
+        float acc[COUTP];
+        tmem_load<COUTP>(tmem + ((uint32_t)(32 * warp) << 16), acc);
+        const int px = x0 + 32 * warp + lane;
+        if (px < W) {
+            const long long o = ((long long)b * (H + 2) + y + 1) * Wp + px + 1;
+            if (MODE == kModeHead) {
+                outf[((long long)b * H + y) * W + px] = acc[0] + bias[0];
+            } else {
+#pragma unroll
+                for (int q = 0; q < COUTP / 8; ++q) {
+                    float v[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) v[e] = acc[8 * q + e];
+                    if (MODE == kModeGelu || MODE == kModeGeluRes) {
+                        uint32_t pk[4];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) v[e] += bias[8 * q + e];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            pk[e] = pack2(__float2bfloat16(v[2 * e]), __float2bfloat16(v[2 * e + 1]));
+                        *reinterpret_cast<uint4 *>(pre + o * COUTP + 8 * q) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) v[e] = gelu(v[e]);
+                    }
+                    if ((MODE == kModeGeluRes || MODE == kModeLinear) && res) {
+                        const uint4 rv = *reinterpret_cast<const uint4 *>(res + o * COUTP + 8 * q);
+                        const uint32_t rw[4] = {rv.x, rv.y, rv.z, rv.w};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            v[2 * e] += __bfloat162float(__ushort_as_bfloat16((unsigned short)(rw[e] & 0xFFFFu)));
+                            v[2 * e + 1] += __bfloat162float(__ushort_as_bfloat16((unsigned short)(rw[e] >> 16)));
+                        }
+                    }
+                    uint32_t pk[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) pk[e] = pack2(__float2bfloat16(v[2 * e]), __float2bfloat16(v[2 * e + 1]));
+                    *reinterpret_cast<uint4 *>(out + o * COUTP + 8 * q) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+}
+
 // dpre = dh * gelu'(pre) over the interior (halo left at zero)
 __global__ void k_gelu_back(const bf16 *__restrict__ dh, const bf16 *__restrict__ pre,
                             bf16 *__restrict__ dpre, int C, int B, int H, int W) {
@@ -295,14 +524,24 @@ __global__ void k_gather(const float *__restrict__ fields, const int *__restrict
     }
 }
 
+// which kernel tl_nn_conv runs: the tcgen05 one (default) or mma.sync
+bool g_conv_tcgen05 = true;
+
 template <int CIN, int COUTP, int MODE>
 int launch_conv(const void *in, const void *w, const float *bias, const void *res, void *out, void *pre,
                 float *outf, int B, int H, int W, cudaStream_t s) {
-    const long long tasks = (long long)B * H * (W / 16);
-    const unsigned grid = (unsigned)((tasks + 3) / 4);
-    k_conv<CIN, COUTP, MODE><<<grid, 128, 0, s>>>((const bf16 *)in, (const bf16 *)w, bias,
-                                                  (const bf16 *)res, (bf16 *)out, (bf16 *)pre, outf, B,
-                                                  H, W);
+    if (g_conv_tcgen05) {
+        const long long tiles = (long long)B * H * ((W + kTcPix - 1) / kTcPix);
+        k_conv_tc<CIN, COUTP, MODE><<<(unsigned)tiles, 128, 0, s>>>((const bf16 *)in, (const bf16 *)w, bias,
+                                                                    (const bf16 *)res, (bf16 *)out, (bf16 *)pre,
+                                                                    outf, B, H, W);
+    } else {
+        const long long tasks = (long long)B * H * (W / 16);
+        const unsigned grid = (unsigned)((tasks + 3) / 4);
+        k_conv<CIN, COUTP, MODE><<<grid, 128, 0, s>>>((const bf16 *)in, (const bf16 *)w, bias,
+                                                      (const bf16 *)res, (bf16 *)out, (bf16 *)pre, outf, B,
+                                                      H, W);
+    }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? TL_OK : cuda_fail(e, "conv launch");
 }
@@ -333,6 +572,25 @@ int tl_nn_conv(int mode, int cin, int coutp, const void *in, const void *w, cons
 #undef TL_CONV_CASE
     set_error("tl_nn_conv: unsupported shape cin=%d coutp=%d mode=%d", cin, coutp, mode);
     return TL_ERR_ARG;
+}
+
+int tl_nn_set_conv_kernel(int tcgen05) {
+    g_conv_tcgen05 = tcgen05 != 0;
+    return TL_OK;
+}
+
+int tl_nn_conv_status(void) {
+    int flag = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&flag, g_conv_tc_error, sizeof flag);
+    if (e != cudaSuccess) return cuda_fail(e, "tl_nn_conv_status");
+    if (flag) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbol(g_conv_tc_error, &zero, sizeof zero);
+        if (e != cudaSuccess) return cuda_fail(e, "tl_nn_conv_status");
+        set_error("tcgen05 conv: the wait for the tensor-core result ran out");
+        return TL_ERR_CUDA;
+    }
+    return TL_OK;
 }
 
 int tl_nn_gelu_backward(const void *dh, const void *pre, void *dpre, int C, int B, int H, int W, void *stream) {

@@ -64,6 +64,12 @@ constexpr int kMaxDirs = kHist + 1; // + the network's direction
 constexpr int kGramPairs = kMaxDirs * (kMaxDirs + 1) / 2;
 constexpr int kGramSums = kGramPairs + kMaxDirs + 1;  // d_i.Ad_j (i <= j), d_i.r0, r0.r0
 constexpr float kClamp = 64.f;      // bound of the scaled inputs
+// The network is consulted while it pays: when its direction adds less than
+// kNetMinShare of the joint projection's energy decrease, the next
+// kNetSkip solves start from the increment history alone (its inference
+// and Gram sums cost a few per cent of a solve), then it is tried again.
+constexpr double kNetMinShare = 0.01;
+constexpr int kNetSkip = 8;
 
 struct Warm {
     // previous-step tracking (both warm start modes)
@@ -79,6 +85,7 @@ struct Warm {
     double *partials;           // [kGramBlocks][kGramSums]
     float *scale;               // device [0] max|u^n|, [1] max|r0|
     bool have_prev;             // u^(n-1) is known
+    int net_skip;               // solves left before the network is consulted again
     std::vector<void *> allocs;
     // the network (learned mode)
     bool model;
@@ -458,6 +465,7 @@ void warm_free(Chunk *c) {
 void warm_reset(Chunk *c) {
     if (Warm *w = warm_of(c)) {
         w->have_prev = false;
+        w->net_skip = 0;
         w->nhist = w->head = w->cur = 0;
     }
 }
@@ -520,6 +528,7 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
     }
     info->warm_used = 0;
     info->warm_ratio = 1.0;
+    info->warm_net_share = 0.0;
     cudaStream_t s = c->stream;
     // the plain start u = u^n: r = u^n - A u^n, its norm defines the exit test
     if ((rc = launch_residual(c, kEpiStore))) return rc;
@@ -548,7 +557,9 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
     Dirs D = H;
     Coefs C = CH;
     double gain = gh;
-    if (learned) {
+    const bool consult = learned && w->net_skip == 0;
+    if (learned && !consult) w->net_skip--;
+    if (consult) {
         // the network corrects u_h: input r_h = u^n - A u_h; then the joint
         // projection over its direction and the increments
         k_resid_of<<<1216, 256, 0, s>>>(c->g, c->u0, w->ustart, c->diag, c->kx, c->ky, w->rh);
@@ -559,6 +570,8 @@ int warm_start_or_fallback(Chunk *c, tl_solve_info_t *info, double *r0, double *
         D.d[D.n++] = w->dnet;
         for (int j = 0; j < w->nhist; ++j) D.d[D.n++] = w->hist[(w->cur - j + kHist) % kHist];
         if ((rc = gram_project(c, w, D, &C, &gain))) return rc;
+        info->warm_net_share = gain > 0.0 && gain >= gh ? (gain - gh) / gain : 0.0;
+        if (!(info->warm_net_share > kNetMinShare)) w->net_skip = kNetSkip;
         if (!(gain >= gh)) {
             // the network's direction is unusable (not finite, e.g. a model
             // of NaNs) or adds nothing: fall back to the history start

@@ -8,7 +8,7 @@ Chebyshev runs at tl_eps 1e-10: at 1e-15 it measures the true residual,
 whose FP64 floor lies above 1e-15 * ||r_0|| on these grids, so every step
 would run to tl_max_iters and its iteration counts would pin nothing.
 
-Every step record also carries u at a 16 x 16 lattice of interior cells
+Every step record carries the field summary and u at a 16 x 16 lattice of interior cells
 (`u_samples`, tea_oracle --u-samples), against which the mixed-precision
 solves report their per-timestep pointwise error.
 
@@ -45,7 +45,8 @@ U_SAMPLES = 16
 
 
 def deck_for(n, method, steps=STEPS):
-    return decks.make_deck(n=n, end_step=steps, **METHODS[method])
+    # a field summary every timestep (it only reads the fields)
+    return decks.make_deck(n=n, end_step=steps, summary_frequency=1, **METHODS[method])
 
 
 def main():

@@ -58,7 +58,7 @@ def _u_samples(ch, n, s):
 def run_against_golden(n, method, mixed=False):
     """timestep by timestep through the tl_* API; returns per-step errors"""
     g, m = _method(n, method)
-    deck = decks.make_deck(n=n, end_step=m["end_step"], **m["deck_params"])
+    deck = decks.make_deck(n=n, end_step=m["end_step"], summary_frequency=1, **m["deck_params"])
     if mixed:
         deck = deck.replace("*endtea", "tl_precision mixed\n*endtea")
     gold = m["steps"]

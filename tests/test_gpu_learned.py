@@ -112,3 +112,56 @@ def test_warm_start_with_mixed_ppcg_keeps_the_fp64_answer(mode):
             assert info["warm_used"] == 1, step  # an increment exists from the second step on
         for a, b in zip(fs, ref["summary"]):
             assert a == pytest.approx(b, rel=1e-10), step
+
+
+@pytest.mark.parametrize("W", [144, 256])
+@pytest.mark.parametrize("shape", [(16, 32, 0), (32, 32, 1), (32, 32, 0), (32, 16, 2), (32, 32, 3), (16, 32, 3)])
+def test_tcgen05_conv_matches_mma_sync_conv(shape, W):
+    """The tensor-memory (tcgen05) convolution and the warp-level mma.sync
+    one compute the same BF16 products with FP32 accumulation in another
+    order: their BF16 outputs agree to one BF16 rounding (2^-8 relative),
+    on a width that is a multiple of the 128-pixel tile and on one that is
+    not (a partial last tile)."""
+    import ctypes as C
+    lib = tl.load()
+    lib.tl_nn_set_conv_kernel.argtypes = [C.c_int]
+    cin, co, mode = shape
+    B, H = 2, 5
+    g = torch.Generator().manual_seed(cin * 100 + co * 10 + mode + W)
+    dev = "cuda:0"
+    x = torch.zeros(B, H + 2, W + 2, cin)
+    x[:, 1:-1, 1:-1, :] = torch.randn(B, H, W, cin, generator=g)
+    x = x.to(torch.bfloat16).to(dev)
+    wt = (0.2 * torch.randn(9, co, cin, generator=g)).to(torch.bfloat16).to(dev)
+    bias = (0.1 * torch.randn(co, generator=g)).to(dev)
+    res = torch.zeros(B, H + 2, W + 2, co)
+    res[:, 1:-1, 1:-1, :] = torch.randn(B, H, W, co, generator=g)
+    res = res.to(torch.bfloat16).to(dev)
+    outs = {}
+    for tc in (1, 0):
+        out = torch.zeros(B, H + 2, W + 2, co, dtype=torch.bfloat16, device=dev)
+        pre = torch.zeros_like(out)
+        outf = torch.zeros(B, H, W, device=dev)
+        assert lib.tl_nn_set_conv_kernel(tc) == 0
+        rc = lib.tl_nn_conv(mode, cin, co, x.data_ptr(), wt.data_ptr(), bias.data_ptr(),
+                            res.data_ptr() if mode in (1, 3) else None, out.data_ptr(), pre.data_ptr(),
+                            outf.data_ptr(), B, H, W, None)
+        assert rc == 0, tl.last_error()
+        torch.cuda.synchronize()
+        assert lib.tl_nn_conv_status() == 0, tl.last_error()
+        outs[tc] = (out.float().cpu().numpy(), pre.float().cpu().numpy(), outf.cpu().numpy())
+    lib.tl_nn_set_conv_kernel(1)
+    for a, b in zip(outs[1], outs[0]):
+        assert np.all(np.abs(a - b) <= 2.0 ** -7 * np.abs(b) + 1e-6), (shape, W, float(np.max(np.abs(a - b))))
+    # and against a float64 convolution of the same BF16 inputs
+    xs, ws = x.double().cpu().numpy(), wt.double().cpu().numpy()
+    ref = np.zeros((B, H, W, co))
+    for tap in range(9):
+        dy, dx = divmod(tap, 3)
+        ref += np.einsum("bhwc,oc->bhwo", xs[:, dy:dy + H, dx:dx + W, :], ws[tap])
+    ref += bias.double().cpu().numpy()
+    got = outs[1][2] if mode == 2 else outs[1][1][:, 1:-1, 1:-1, :] if mode in (0, 1) else None
+    if mode == 2:
+        assert np.allclose(got, ref[..., 0], rtol=1e-4, atol=1e-4)
+    elif got is not None:
+        assert np.all(np.abs(got - ref) <= 2.0 ** -8 * np.abs(ref) + 1e-5)
