@@ -65,6 +65,9 @@ extern "C" {
 #define TL_WARM_NONE             0  /* u = u^n, the reference's start        */
 #define TL_WARM_LEARNED          1  /* network + previous increment, Galerkin */
 #define TL_WARM_PREV             2  /* previous increment, Galerkin          */
+/* the inner product of the warm start's projection (tl_set_warm_start_options) */
+#define TL_WARM_PROJ_ENERGY      0  /* minimise the energy (A-norm of the error) */
+#define TL_WARM_PROJ_RESIDUAL    1  /* minimise the residual's 2-norm        */
 /* field ids: FIELD_* of data.f90:44-50 plus solver work arrays */
 #define TL_FIELD_DENSITY         1
 #define TL_FIELD_ENERGY0         2
@@ -252,6 +255,11 @@ int tl_dot_noalloc(const double *a, const double *b, int nx, int ny, long long p
  * the 8 bytes "TLWS0001", an int64 parameter count, then the FP32
  * parameters. */
 long long tl_warm_start_param_count(void);
+/* how the warm start combines its directions: the last `history` (1..8,
+ * default 8) increments u^(n-j+1) - u^(n-j), projected in the inner product
+ * `projection` (TL_WARM_PROJ_ENERGY, the default, or TL_WARM_PROJ_RESIDUAL).
+ * A change restarts the history; a loaded model is kept. */
+int tl_set_warm_start_options(tl_chunk_t *ch, int history, int projection);
 int tl_set_warm_start_model(tl_chunk_t *ch, const float *params, long long n);
 /* training data of the step just solved (which must have run with a warm
  * start, so that the increments are tracked): FP32 [ny][nx][8] at device

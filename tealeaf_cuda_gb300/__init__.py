@@ -26,6 +26,7 @@ SOLVER_JACOBI, SOLVER_CG, SOLVER_CHEBYSHEV, SOLVER_PPCG = 1, 2, 3, 4
 PREC_NONE, PREC_JAC_DIAG, PREC_JAC_BLOCK = 1, 2, 3
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 WARM_NONE, WARM_LEARNED, WARM_PREV = 0, 1, 2
+WARM_PROJ_ENERGY, WARM_PROJ_RESIDUAL = 0, 1
 FIELDS = {"density": 1, "energy0": 2, "energy1": 3, "u": 4, "p": 5, "sd": 6, "r": 7,
           "u0": 8, "w": 9, "z": 10, "kx": 11, "ky": 12, "mi": 13, "cp": 14, "bfp": 15,
           "volume": 16, "rtemp": 17, "utemp": 18, "r_store": 19}
@@ -160,6 +161,7 @@ def load():
     lib.tl_run_deck.argtypes = [C.c_char_p, C.POINTER(RunOptions), C.POINTER(RunResult)]
     lib.tl_warm_start_param_count.restype = C.c_longlong
     lib.tl_set_warm_start_model.argtypes = [C.c_void_p, C.c_void_p, C.c_longlong]
+    lib.tl_set_warm_start_options.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.tl_warm_start_features.argtypes = [C.c_void_p, C.c_void_p]
     _vp, _i, _f = C.c_void_p, C.c_int, C.c_float
     lib.tl_nn_conv.argtypes = [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _vp]
@@ -242,6 +244,11 @@ class Chunk:
         v = [C.c_double() for _ in range(4)]
         _check(load().tl_start(self._h, *[C.byref(x) for x in v]), "tl_start")
         return tuple(x.value for x in v)
+
+    def set_warm_start_options(self, history=8, projection=WARM_PROJ_ENERGY):
+        """increments the warm start combines (1..8) and its projection's
+        inner product (WARM_PROJ_ENERGY or WARM_PROJ_RESIDUAL)"""
+        _check(load().tl_set_warm_start_options(self._h, history, projection), "tl_set_warm_start_options")
 
     def set_dt(self, dt):
         _check(load().tl_set_dt(self._h, dt), "tl_set_dt")

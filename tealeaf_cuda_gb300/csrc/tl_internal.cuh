@@ -137,6 +137,8 @@ struct Chunk {
     int sms;                     // multiprocessors of the device
     // learned warm start model and buffers (tl_warm.cu)
     void *warm;
+    int warm_history;            // previous increments the warm start combines (1..8)
+    int warm_projection;         // TL_WARM_PROJ_*: energy (Galerkin) or minimal residual
     double rx, ry;
     // per-kernel profiling (CUDA events around eager launches)
     bool profiling;
@@ -246,6 +248,7 @@ constexpr int kInnerSegDefault = 0;
 void warm_free(Chunk *c);
 void warm_reset(Chunk *c);                // forget u^(n-1) (tl_start)
 long long warm_param_count();
+int warm_set_options(Chunk *c, int history, int projection);
 int warm_set_model(Chunk *c, const float *params, long long n);
 bool warm_ready(Chunk *c);                // a network is loaded
 int warm_features(Chunk *c, float *dst);  // [ny][nx][8] inputs + target

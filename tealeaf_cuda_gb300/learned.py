@@ -9,7 +9,7 @@ alone, u_h; inputs (u^n / max|u^n|, log density, log1p Kx, log1p Ky,
 d_1 = u^n - u^{n-1}; six 3x3 convolutions of 32 channels (GELU, four
 residual blocks); output (u^{n+1} - u_h) / max|r_h|.  The solve starts from
 u^n plus the energy-minimising combination of the network's output and the
-last four increments, and keeps tl_eps * (plain start residual) as its exit
+last eight increments, and keeps tl_eps * (plain start residual) as its exit
 test.  Torch only allocates
 device buffers here; every FLOP of the network runs in the library's
 kernels.
