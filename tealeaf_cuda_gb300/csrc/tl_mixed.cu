@@ -800,9 +800,12 @@ __device__ __forceinline__ float row_of(const float4 &v, int k) {
 // LAST: the last pass of a solve (writes z in FP64).  FIRST: the first pass
 // of a solve, which starts the inner steps from r (FP64): rtemp = r, sd =
 // utemp = M^-1 r / theta (the start BodyPpUr<PC, true> writes), instead of
-// reading sd, rtemp and utemp
-template <int T, int PC, bool LAST, bool FIRST>
+// reading sd, rtemp and utemp.  RRN (with LAST only): the pass also sums
+// the outer (r - r_store).z (a template flag, so that passes without the sum
+// carry none of its registers)
+template <int T, int PC, bool LAST, bool FIRST, bool RRN = false>
 __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs a, DevScalars *sc) {
+    static_assert(!RRN || LAST, "the rrn sum belongs to the last pass");
     if (*(volatile const int *)&sc->done) return;
     constexpr int NT = fused_threads<T>();
     constexpr int SR = NT + 2;  // shared-memory row stride
@@ -1064,7 +1067,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                                     const int i64 = cbase + (row + a.h) * a.pitch64;
                                     const double zv = (double)oU[k];
                                     a.z64[i64] = zv;
-                                    if (a.rrn) racc = fma(a.r64[i64] - a.rs64[i64], zv, racc);
+                                    if (RRN) racc = fma(a.r64[i64] - a.rs64[i64], zv, racc);
                                 } else {
                                     const int i = cbase + (row + a.h) * a.pitch;
                                     a.sd_out[i] = oS[k];
@@ -1096,7 +1099,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
             }
         }
     }
-    if (LAST && a.rrn) fused_rrn_reduce(racc, a.partials, a.counter, sc);
+    if (RRN) fused_rrn_reduce(racc, a.partials, a.counter, sc);
 }
 
 // FP32 copies of the preconditioner: Mi = 1/diag, block cp, and bfp with
@@ -1394,16 +1397,24 @@ int mixed_ppcg_prepare(Chunk *c) {
     });
 }
 
-template <int T, int PC, bool LAST, bool FIRST>
-void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, DevScalars *sc) {
+template <int T, int PC, bool LAST, bool FIRST, bool RRN>
+void launch_fused2(dim3 grid, cudaStream_t s, const PpFusedArgs &a, DevScalars *sc) {
     constexpr size_t bytes = fused_smem<T, PC>();
     static bool configured = false;  // the attribute belongs to the kernel: set once
     if (!configured) {
-        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST, FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST, FIRST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST, FIRST, RRN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes);
+        cudaFuncSetAttribute(k_pp_fused<T, PC, LAST, FIRST, RRN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             100);
         configured = true;
     }
-    k_pp_fused<T, PC, LAST, FIRST><<<grid, fused_threads<T>(), bytes, s>>>(a, sc);
+    k_pp_fused<T, PC, LAST, FIRST, RRN><<<grid, fused_threads<T>(), bytes, s>>>(a, sc);
+}
+
+template <int T, int PC, bool LAST, bool FIRST>
+void launch_fused1(dim3 grid, cudaStream_t s, const PpFusedArgs &a, DevScalars *sc) {
+    if (LAST && a.rrn) launch_fused2<T, PC, LAST, FIRST, LAST>(grid, s, a, sc);
+    else launch_fused2<T, PC, LAST, FIRST, false>(grid, s, a, sc);
 }
 
 template <int T, int PC>
@@ -1682,6 +1693,7 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
     double rn_prev = 0.0;
     int outer = 0, inner_total = 0;
     int status = TL_OK;
+    bool capped = false;  // an inner solve stopped at tl_max_iters before tl_inner_eps
     while (true) {
         if (isnan(rn)) {  // a NaN residual never meets the tests below
             set_error("mixed solve: breakdown (NaN in the FP64 residual) after %d refinement steps", outer);
@@ -1690,14 +1702,15 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
         }
         if (rn < target) break;
         if (outer > 0 && rn > 0.5 * rn_prev) break;  // FP64 residual floor reached
-        if (outer >= kMaxOuter || inner_total >= cf.max_iters) {
+        if (outer >= kMaxOuter) {
             status = TL_WARN_MAXITER;
             break;
         }
-        // inner FP32 PCG on A d = r
+        // inner FP32 PCG on A d = r; tl_max_iters bounds each inner solve as
+        // it bounds one CG solve of the FP64 path
         h.done = kRunning;
         h.in_target = cf.inner_eps;
-        h.in_max = cf.max_iters - inner_total;
+        h.in_max = cf.max_iters;
         if ((rc = chunk_push_scalars(c))) return rc;
         if (diag) {
             BodyInnerInit<TL_PREC_JAC_DIAG> bi{c->r, mx->mi, mx->ky, mx->cp, mx->bfp, mx->r, mx->z, mx->p, mx->d,
@@ -1716,6 +1729,7 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
             break;
         }
         inner_total += h.in_n;
+        if (h.in_n >= cf.max_iters) capped = true;
         // u += d (FP64), r = u0 - A u (FP64)
         BodyUpdateU bu{c->u, mx->d, c->pitch, c->pitch};
         if ((rc = run32(c, "mixed_update_u", bu, kInNone, false))) return rc;
@@ -1724,6 +1738,10 @@ int solve_timestep_mixed(Chunk *c, tl_solve_info_t *info) {
         rn_prev = rn;
         rn = sqrt(fabs(h.sum[0]));
         outer++;
+    }
+    if (capped && status == TL_OK) {
+        status = TL_WARN_MAXITER;
+        set_error("mixed solve: an inner FP32 solve reached tl_max_iters (%d) before tl_inner_eps", cf.max_iters);
     }
     info->status = status;
     info->outer_iters = outer;

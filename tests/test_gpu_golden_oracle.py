@@ -28,9 +28,11 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FS_RTOL = 1e-10
-# u at a cell of two FP64 solves that each meet tl_eps 1e-15 (summed in
-# different orders): measured differences are ~1e-13 of max|u|
-U_RTOL = 1e-9
+# u at a cell of two FP64 solves that each meet tl_eps 1e-15 (their sums run
+# in different orders): measured differences are below 2e-14 of max|u| at
+# 1024^2; the mixed-precision solves differ from the FP64 oracle by up to
+# 3e-13 of max|u| and 4e-13 in the field summary
+U_RTOL = 1e-11
 SUMMARY = ("vol", "mass", "ie", "temp")
 
 

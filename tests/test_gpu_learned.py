@@ -20,6 +20,13 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
+# The oracle rounds activations and gradients to BF16 at the kernels'
+# rounding points but accumulates in FP64; the kernels accumulate in FP32 in
+# another order, so a value next to a BF16 rounding boundary can round the
+# other way and carry a 2^-8 relative difference into the layers below it.
+GRAD_RTOL = 3e-2
+
+
 def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
@@ -55,12 +62,16 @@ def test_gradients_match_oracle():
     _, dy = nn.loss_and_dy(yo, t, 4, quant=True)
     grads = nn.backward(params.astype(np.float64), cache, dy, quant=True)
     off = 0
+    errs = []
     for li, ((cin, co, _), (dw, db)) in enumerate(zip(nn.LAYERS, grads)):
         nw = 9 * co * cin
         gw, gb = g[off:off + nw].reshape(9, co, cin), g[off + nw:off + nw + co]
-        assert _rel(gw, dw) < 3e-2, (li, _rel(gw, dw))
-        assert _rel(gb, db) < 3e-2, (li, _rel(gb, db))
+        errs.append((li, _rel(gw, dw), _rel(gb, db)))
         off += nw + co
+    print("\nlayer, weight-gradient and bias-gradient relative error against the oracle:", errs)
+    for li, ew, eb in errs:
+        assert ew < GRAD_RTOL, (li, ew)
+        assert eb < GRAD_RTOL, (li, eb)
 
 
 def test_training_and_warm_start_gain():
