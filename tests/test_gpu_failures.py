@@ -6,7 +6,8 @@ status instead and leave the context usable:
   * a warm-start model of NaNs: the network's direction is dropped and the
     solve starts from the increment history (or from u = u^n on the first
     step), with the same answer as without the network;
-  * tl_max_iters reached: TL_WARN_MAXITER with the iterations done;
+  * tl_max_iters reached: TL_WARN_MAXITER with the iterations done (for
+    mixed CG: an FP32 inner solve reached it);
   * a NaN in the deck's data (one cell of energy set from the host): the
     Krylov scalars turn NaN and the solve stops with TL_ERR_BREAKDOWN at its
     first exit test instead of carrying the NaN to tl_max_iters;
@@ -78,7 +79,10 @@ def test_max_iters_reports_a_warning(method):
     info = ch.timestep()
     ch.close()
     assert info["status"] == tl.TL_WARN_MAXITER
-    assert info["error_ratio"] > 1e-15
+    if not mixed:
+        assert info["error_ratio"] > 1e-15  # stopped short of tl_eps
+    # (mixed CG: tl_max_iters bounds each FP32 inner solve; the FP64
+    # refinement around the capped inner solves may still reach tl_eps)
 
 
 @pytest.mark.parametrize("method", [
