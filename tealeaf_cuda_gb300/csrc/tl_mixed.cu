@@ -841,16 +841,20 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
         const bool own = incol && tid >= T && tid < T + a.band;
         // the pipeline registers carried from one strip to the next: per
         // producer level l < T its output strip of the previous iteration
-        // (sd, rtemp, utemp) and the last sd row of the one before, and
-        // level 0's loads of the next strip.  For T <= 3 the strip loop is
-        // unrolled by two with two sets that swap roles, so nothing is
-        // copied from one set to the other.
+        // (sd, rtemp, utemp) and the last sd row of the one before.  For
+        // T <= 3 the strip loop is unrolled by two with two sets that swap
+        // roles, so nothing is copied from one set to the other.  Level 0's
+        // loads of the next strip are one set (Ld): an iteration has used
+        // them up before it loads the next strip into them.
         struct Pipe {
             float sdP[T][4], sdL[T], rtP[T][4], utP[T][4];
+        };
+        struct Ld {
             float ldS[4], ldR[4], ldU[4], ldC[NA][4];
             double ldR64[FIRST ? 4 : 1];  // FIRST: r (FP64) in place of sd, rtemp, utemp
         };
         Pipe pa, pb;
+        Ld ld;
 #pragma unroll
         for (int l = 0; l < T; ++l) {
             pa.sdL[l] = 0.f;
@@ -860,7 +864,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
         // level 0 loads, one strip ahead (32-bit offsets, FP64 fields too: a
         // field has < 2^31 elements)
         const int cbase = col + a.h;
-        auto load = [&](int s, Pipe &o) {
+        auto load = [&](int s, Ld &o) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const int row = 4 * s + k;
@@ -913,7 +917,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                 }
             }
         };
-        load(sb - T, pa);
+        load(sb - T, ld);
 #pragma unroll
         for (int d = 1; d <= kFusedPrefetch; ++d) prefetch(sb - T + d);
         int slot = (sb - T + 8 * R) % R;  // ring slot of strip s (sb - T >= -2T >= -8)
@@ -932,31 +936,31 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                 float zf[4];
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    r0[k] = (float)in.ldR64[k];
+                    r0[k] = (float)ld.ldR64[k];
                     zf[k] = 0.f;
                 }
                 if constexpr (PC == TL_PREC_JAC_BLOCK) {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
                         if (k < mm)
-                            zf[k] = k == 0 ? r0[0] * in.ldC[3][0]
-                                           : fmaf(in.ldC[1][k], zf[k > 0 ? k - 1 : 0], r0[k]) * in.ldC[3][k];
+                            zf[k] = k == 0 ? r0[0] * ld.ldC[3][0]
+                                           : fmaf(ld.ldC[1][k], zf[k > 0 ? k - 1 : 0], r0[k]) * ld.ldC[3][k];
 #pragma unroll
                     for (int k = 2; k >= 0; --k)
-                        if (k < mm - 1) zf[k] = fmaf(-in.ldC[2][k], zf[k + 1], zf[k]);
+                        if (k < mm - 1) zf[k] = fmaf(-ld.ldC[2][k], zf[k + 1], zf[k]);
                 } else {
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
-                        if (k < mm) zf[k] = PC == TL_PREC_JAC_DIAG ? r0[k] * in.ldC[NA - 1][k] : r0[k];
+                        if (k < mm) zf[k] = PC == TL_PREC_JAC_DIAG ? r0[k] * ld.ldC[NA - 1][k] : r0[k];
                 }
 #pragma unroll
                 for (int k = 0; k < 4; ++k) s0[k] = u0[k] = k < mm ? zf[k] * theta_r : 0.f;
             } else {
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    s0[k] = in.ldS[k];
-                    r0[k] = in.ldR[k];
-                    u0[k] = in.ldU[k];
+                    s0[k] = ld.ldS[k];
+                    r0[k] = ld.ldR[k];
+                    u0[k] = ld.ldU[k];
                 }
             }
             {
@@ -964,9 +968,9 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                 xsb[(s & 1) * SR + tid] = make_float4(s0[0], s0[1], s0[2], s0[3]);
 #pragma unroll
                 for (int q = 0; q < NA; ++q)
-                    cf[q * SR] = make_float4(in.ldC[q][0], in.ldC[q][1], in.ldC[q][2], in.ldC[q][3]);
+                    cf[q * SR] = make_float4(ld.ldC[q][0], ld.ldC[q][1], ld.ldC[q][2], ld.ldC[q][3]);
             }
-            if (s + 1 < s_end) load(s + 1, out);
+            if (s + 1 < s_end) load(s + 1, ld);
             if (s + 1 + kFusedPrefetch < s_end) prefetch(s + 1 + kFusedPrefetch);
             // levels 1..T; FULL: every level's strip lies in the field and has 4
             // rows, so no level tests rows (columns outside the field compute on
