@@ -492,11 +492,17 @@ def run_ours(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_its = []
+    t_in = t_solve = t_out = 0.0  # host wall time of the copies in, the solves, the copy out
     for _ in range(K):
+        ta = time.perf_counter()
         ch.set_field("density", host_rho)
         ch.set_field("energy1", host_e)
+        tb = time.perf_counter()
         e2e_its.append(ch.timestep()["iterations"])
+        tc = time.perf_counter()
         ch.get_field("energy1", out=host_e)
+        td = time.perf_counter()
+        t_in, t_solve, t_out = t_in + (tb - ta), t_solve + (tc - tb), t_out + (td - tc)
     torch.cuda.synchronize()
     e2e_s = allreduce_max(time.perf_counter() - t0, ws, local)
     ch.close()
@@ -533,7 +539,8 @@ def run_ours(args):
     work = allreduce_sum(float(cells * sum(its_p)), ws, local)
     value = work / (ms_max * 1e-3)
     e2e = {"value": work / e2e_s, "unit": "plain-CG cell-iters/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / K, "iterations_per_step": e2e_its}
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / K, "iterations_per_step": e2e_its,
+           "ms_per_step_h2d_solve_d2h": [1e3 * t_in / K, 1e3 * t_solve / K, 1e3 * t_out / K]}
     rel = [abs(a - b) / abs(b) if b else abs(a) for a, b in zip(summary_h, summary_p)]
     rel_steps = [max(abs(a - b) / abs(b) if b else abs(a) for a, b in zip(x, y)) for x, y in zip(sums_h, sums_p)]
 
