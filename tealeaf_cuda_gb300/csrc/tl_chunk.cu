@@ -361,10 +361,12 @@ void drop_graphs(Chunk *c) {
         }
 }
 
-// Host copies of a field move as one contiguous block through a device
-// staging buffer (rows x (nx + 2h), the host layout), re-pitched by a
-// kernel: a pitched 2-D copy moves one short row at a time and runs far
-// below the host link's bandwidth.
+// Host copies of a field: from page-locked, mapped host memory a kernel
+// reads (or writes) the host array directly and re-pitches it in the same
+// pass; from other host memory the field moves as one contiguous block
+// through a device staging buffer (rows x (nx + 2h), the host layout) that
+// a kernel re-pitches.  (A pitched 2-D copy moves one short row at a time
+// and runs far below the host link's bandwidth.)
 // to_pitched: dst[r * pitch + c] = src[r * w + c]; else the reverse
 static __global__ void k_repitch(double *__restrict__ dst, const double *__restrict__ src, int w, int pitch,
                           int rows, bool to_pitched) {
@@ -375,6 +377,19 @@ static __global__ void k_repitch(double *__restrict__ dst, const double *__restr
             else dst[dense + col] = src[pitched + col];
         }
     }
+}
+
+// the device address of page-locked, mapped host memory (cudaHostAlloc /
+// cudaHostRegister), or nullptr for any other host pointer: a kernel then
+// moves the field between HBM and the host in one pass, re-pitching as it
+// goes, instead of a DMA copy through the staging buffer
+static void *mapped_host(const void *host) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();  // an unregistered pointer is not an error here
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
 static int stage_buffer(Chunk *c, double **out) {
@@ -531,8 +546,13 @@ int tl_get_field(tl_chunk_t *ch, int field, double *host) {
     Chunk *c = ch->c;
     const int w = c->nx + 2 * c->h;
     const size_t bytes = (size_t)w * (size_t)c->rows * sizeof(double);
+    double *mapped = (double *)mapped_host(host);
     if (w == c->pitch) {
         TL_CUDA(cudaMemcpyAsync(host, f, bytes, cudaMemcpyDeviceToHost, c->stream));
+    } else if (mapped) {
+        k_repitch<<<c->sms * 8, 256, 0, c->stream>>>(mapped, f, w, c->pitch, c->rows, false);
+        TL_CUDA(cudaGetLastError());
+        c->launches++;
     } else {
         double *st;
         if ((rc = stage_buffer(c, &st))) return rc;
@@ -552,8 +572,13 @@ int tl_set_field(tl_chunk_t *ch, int field, const double *host) {
     Chunk *c = ch->c;
     const int w = c->nx + 2 * c->h;
     const size_t bytes = (size_t)w * (size_t)c->rows * sizeof(double);
+    const double *mapped = (const double *)mapped_host(host);
     if (w == c->pitch) {
         TL_CUDA(cudaMemcpyAsync(f, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    } else if (mapped) {
+        k_repitch<<<c->sms * 8, 256, 0, c->stream>>>(f, mapped, w, c->pitch, c->rows, true);
+        TL_CUDA(cudaGetLastError());
+        c->launches++;
     } else {
         double *st;
         if ((rc = stage_buffer(c, &st))) return rc;
