@@ -24,7 +24,9 @@ torch = pytest.importorskip("torch")
 # rounding points but accumulates in FP64; the kernels accumulate in FP32 in
 # another order, so a value next to a BF16 rounding boundary can round the
 # other way and carry a 2^-8 relative difference into the layers below it.
-GRAD_RTOL = 3e-2
+# Measured (norm-wise, per layer): 1e-5 to 4.8e-4, largest in the first
+# layer, whose gradient passes through every other layer's rounding.
+GRAD_RTOL = 2e-3
 
 
 def _rel(a, b):
