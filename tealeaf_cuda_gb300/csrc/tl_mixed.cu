@@ -797,6 +797,36 @@ __device__ __forceinline__ float row_of(const float4 &v, int k) {
     return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
 }
 
+// Paired FP32 arithmetic (f32x2): two rows of a strip in one instruction,
+// each lane rounded exactly as the scalar operation (round to nearest, no
+// flush to zero), so a paired step gives the scalar step's bits.
+using f2 = unsigned long long;
+__device__ __forceinline__ f2 pk2(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void up2(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// cell_apply on rows (k, k+1): the same four fused steps in the same order
+__device__ __forceinline__ f2 cell_apply2(f2 c, f2 n, f2 s, f2 w, f2 e, f2 kyn, f2 kyc, f2 kxe, f2 kxc) {
+    f2 v = fma2(kyn, sub2(c, n), c);
+    v = fma2(kyc, sub2(c, s), v);
+    v = fma2(kxe, sub2(c, e), v);
+    return fma2(kxc, sub2(c, w), v);
+}
+
 // LAST: the last pass of a solve (writes z in FP64).  FIRST: the first pass
 // of a solve, which starts the inner steps from r (FP64): rtemp = r, sd =
 // utemp = M^-1 r / theta (the start BodyPpUr<PC, true> writes), instead of
@@ -1003,6 +1033,23 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                     // one inner step on the strip's first mm rows (mm == 4: no row tests)
                     auto step = [&](const int mm) {
                         float z[4];
+                        if (mm == 4) {
+                            // a full strip: the stencil of rows (0, 1) and (2, 3) as
+                            // f32x2 pairs (the updates below stay scalar: paired, they
+                            // need more registers and the last pass spills)
+                            const f2 c01 = pk2(x0[0], x0[1]), c23 = pk2(x0[2], x0[3]);
+                            const f2 x12 = pk2(x0[1], x0[2]);  // north of rows 0, 1 and south of rows 2, 3
+                            const f2 r01 = sub2(pk2(in.rtP[t - 1][0], in.rtP[t - 1][1]),
+                                                cell_apply2(c01, x12, pk2(in.sdL[t - 1], x0[0]), pk2(xw4.x, xw4.y),
+                                                            pk2(xe4.x, xe4.y), pk2(ky4.y, ky4.z), pk2(ky4.x, ky4.y),
+                                                            pk2(kxe4.x, kxe4.y), pk2(kx4.x, kx4.y)));
+                            const f2 r23 = sub2(pk2(in.rtP[t - 1][2], in.rtP[t - 1][3]),
+                                                cell_apply2(c23, pk2(x0[3], cS[0]), x12, pk2(xw4.z, xw4.w),
+                                                            pk2(xe4.z, xe4.w), pk2(ky4.w, ky_top), pk2(ky4.z, ky4.w),
+                                                            pk2(kxe4.z, kxe4.w), pk2(kx4.z, kx4.w)));
+                            up2(r01, oR[0], oR[1]);
+                            up2(r23, oR[2], oR[3]);
+                        } else {
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
                             oS[k] = oR[k] = oU[k] = z[k] = 0.f;
@@ -1014,6 +1061,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                                 oR[k] = in.rtP[t - 1][k] - cell_apply(c, n, sv, row_of(xw4, k), row_of(xe4, k), kyn,
                                                                       row_of(ky4, k), row_of(kxe4, k), row_of(kx4, k));
                             }
+                        }
                         }
                         if constexpr (PC == TL_PREC_JAC_BLOCK) {
                             // Thomas: dp0 = x0 / b0, dp_k = (x_k + Ky_k dp_{k-1}) bfp_k,
