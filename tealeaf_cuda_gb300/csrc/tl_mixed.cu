@@ -814,6 +814,16 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
 __device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
     f2 r;
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
@@ -1035,8 +1045,7 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                         float z[4];
                         if (mm == 4) {
                             // a full strip: the stencil of rows (0, 1) and (2, 3) as
-                            // f32x2 pairs (the updates below stay scalar: paired, they
-                            // need more registers and the last pass spills)
+                            // f32x2 pairs
                             const f2 c01 = pk2(x0[0], x0[1]), c23 = pk2(x0[2], x0[3]);
                             const f2 x12 = pk2(x0[1], x0[2]);  // north of rows 0, 1 and south of rows 2, 3
                             const f2 r01 = sub2(pk2(in.rtP[t - 1][0], in.rtP[t - 1][1]),
@@ -1087,11 +1096,23 @@ __global__ void __launch_bounds__(fused_threads<T>(), 2) k_pp_fused(PpFusedArgs 
                             for (int k = 0; k < 4; ++k)
                                 if (k < mm) z[k] = oR[k];
                         }
+                        if (mm == 4 && !LAST) {
+                            // paired updates too, except in the last pass (whose FP64
+                            // stores leave no registers for them)
+                            const f2 al2 = pk2(al[t - 1], al[t - 1]), be2 = pk2(be[t - 1], be[t - 1]);
+                            const f2 s01 = fma2(al2, pk2(x0[0], x0[1]), mul2(be2, pk2(z[0], z[1])));
+                            const f2 s23 = fma2(al2, pk2(x0[2], x0[3]), mul2(be2, pk2(z[2], z[3])));
+                            up2(s01, oS[0], oS[1]);
+                            up2(s23, oS[2], oS[3]);
+                            up2(add2(pk2(in.utP[t - 1][0], in.utP[t - 1][1]), s01), oU[0], oU[1]);
+                            up2(add2(pk2(in.utP[t - 1][2], in.utP[t - 1][3]), s23), oU[2], oU[3]);
+                        } else {
 #pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            if (k < mm) {
-                                oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
-                                oU[k] = in.utP[t - 1][k] + oS[k];
+                            for (int k = 0; k < 4; ++k) {
+                                if (k < mm) {
+                                    oS[k] = fmaf(al[t - 1], x0[k], be[t - 1] * z[k]);
+                                    oU[k] = in.utP[t - 1][k] + oS[k];
+                                }
                             }
                         }
                     };
