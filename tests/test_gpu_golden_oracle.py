@@ -7,8 +7,9 @@ iteration counts within +-1 (Chebyshev +-10: it reads its residual every
 10th iteration, tea_solve.f90:277), field summaries within 1e-10 relative,
 and u at the fixture's 16 x 16 lattice of cells within U_RTOL of max|u|.
 
-Chebyshev runs at tl_eps 1e-10 (at 1e-15 its true-residual test sits on the
-FP64 floor and every step runs to tl_max_iters, which pins nothing).
+Chebyshev runs at tl_eps 1e-10 on 1024^2 and 1e-8 on 4096^2 (at tighter
+tolerances its true-residual test sits on the FP64 floor and its steps run
+to tl_max_iters, which pins nothing); the fixture records the deck it ran.
 
 The mixed-precision solves (FP32 inner iterations inside the FP64 outer
 solve) are held to the same bars against the FP64 oracle: mixed CG + jac_diag
