@@ -5,7 +5,8 @@ oracle's committed golden runs (tests/golden/oracle_config2_{1024,4096}.json,
 made by tests/golden/make_oracle_golden.py), timestep by timestep:
 iteration counts within +-1 (Chebyshev +-10: it reads its residual every
 10th iteration, tea_solve.f90:277), field summaries within 1e-10 relative,
-and u at the fixture's 16 x 16 lattice of cells within U_RTOL of max|u|.
+and u at the fixture's 16 x 16 lattice of cells within U_RTOL of max|u|
+(U_RTOL_MIXED for the mixed-precision solves).
 
 Chebyshev runs at tl_eps 1e-10 on 1024^2 and 1e-8 on 4096^2 (at tighter
 tolerances its true-residual test sits on the FP64 floor and its steps run
@@ -29,11 +30,12 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FS_RTOL = 1e-10
-# u at a cell of two FP64 solves that each meet tl_eps 1e-15 (their sums run
-# in different orders): measured differences are below 2e-14 of max|u| at
-# 1024^2; the mixed-precision solves differ from the FP64 oracle by up to
-# 3e-13 of max|u| and 4e-13 in the field summary
-U_RTOL = 1e-11
+# u at a cell, relative to max|u|: two FP64 solves that each meet tl_eps
+# 1e-15 (their sums run in different orders) differ by at most 3e-14 on
+# these decks; the mixed-precision solves differ from the FP64 oracle by up
+# to 3e-13 at 1024^2 and 9e-12 at 4096^2 (field summaries 5e-12)
+U_RTOL = 1e-12
+U_RTOL_MIXED = 1e-10
 SUMMARY = ("vol", "mass", "ie", "temp")
 
 
@@ -92,7 +94,7 @@ def run_against_golden(n, method, mixed=False):
         if not mixed:
             assert abs(r["iterations"] - r["oracle_iterations"]) <= its_tol, r
         assert r["fs_rel"] < FS_RTOL, r
-        assert r["u_rel"] < U_RTOL, r
+        assert r["u_rel"] < (U_RTOL_MIXED if mixed else U_RTOL), r
     return rows
 
 
