@@ -78,8 +78,11 @@ def test_gradients_match_oracle():
 
 def test_training_and_warm_start_gain():
     """Train on 24 decks at 512^2, then count CG iterations on three held-out
-    decks from the plain start, the increment-history start and the learned one;
-    every start must give the same answer to the solve's tolerance."""
+    decks from the plain start, the increment-history start and the learned
+    one; every start must give the same answer to the solve's tolerance.
+    What the network gains over the method without it (the history start) is
+    printed; measured, it is nothing (282 plain, 272 history, 273 with the
+    network), so the test holds it to within 2 % of the history's count."""
     n, steps = 512, 6
     data, iters = learned.trajectory_crops(range(100, 124), n, steps, crops_per_step=4)
     params, hist = learned.train(data, iters=400, batch=16, crop=144, lr=2e-3, seed=0, log_every=50)
@@ -91,6 +94,7 @@ def test_training_and_warm_start_gain():
           f"residual ratios {[r['learned_ratio'] for r in rows]}")
     assert tot["prev_iterations"] < tot["none_iterations"]
     assert tot["learned_iterations"] < tot["none_iterations"]
+    assert tot["learned_iterations"] <= 1.02 * tot["prev_iterations"]
     for m in ("prev", "learned"):
         assert tot[m + "_max_summary_rel_diff"] < 1e-10
 
